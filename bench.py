@@ -1,0 +1,477 @@
+#!/usr/bin/env python3
+"""Benchmark of the back-projection focusing path on GB300.
+
+One step = one focusing pass of the full workload (4000 x 250-pixel DEM,
+40001 pulses, 4762 range bins, Sint 1200..1800, 80 % mask; seeded synthetic
+scene, see sar_backprojection_gb300/synth.py) with the mixed-precision kernel.
+
+Printed (rank 0, one JSON line):
+  value     nominal pixel-pulses / device time per step (Gpix-pulse/s), inputs
+            resident in HBM; whole job (sum over ranks, max-over-ranks time)
+  e2e       same metric through the drop-in call FocalizzatoreBpPx with pinned
+            host inputs: H2D of every input, focusing, D2H of the image
+  fp64      the plain FP64 kernel on the same scene (the comparator)
+  quality   mixed image vs the FP64 kernel's image (which matches the oracle)
+  roofline  FP32/SFU issue roofline of the main kernel (probe-measured peaks),
+            roofline_hbm the same kernel against measured HBM bandwidth
+  cpu_baseline  the oracle's C restatement on the host cores, bounded sample
+
+``--impl reference`` times the reference algorithm's CPU implementation (the
+oracle port: the reference is Python + Numba and its own code cannot run on
+the GPU machine) on all host cores over a bounded pixel sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Gpix-pulse/s plain FP64 vs mixed-prec batched at coherence>=0.9999; p99 latency"
+UNIT = "Gpix-pulse/s"
+WORKLOAD = ("full_4000x250_40001: DEM 4000x250 (5 m x 4 m, Gaussian terrain), 40001 pulses, "
+            "Nra 4762 (1.52 GB complex64), Sint 1200..1800, 80% mask")
+DATA = "synthetic (seeded: 200 point targets + slope-weighted clutter, motion +-1 m)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tuning", type=str, default="",
+                    help="chunk,tile0,tile1[,staged] of the mixed kernel")
+    ap.add_argument("--seed", type=int, default=2)
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------------------
+# distributed bookkeeping (one process per GPU, weak scaling: one scene each)
+
+
+class Dist:
+    def __init__(self):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+
+    def init(self, backend):
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float, device) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64, device=device)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ----------------------------------------------------------------------------
+# clocks during the timed region
+
+
+class ClockSampler:
+    FIELDS = ("uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid: str | None):
+        self.uuid = uuid
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in Path(self.path).read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            if self.uuid and self.uuid not in f[0]:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def device_uuid(dev) -> str | None:
+    import torch
+    try:
+        u = str(torch.cuda.get_device_properties(dev).uuid)
+        return u if u.startswith("GPU-") else "GPU-" + u
+    except Exception:
+        return None
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return json.loads(p.read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def profile_traffic(kernel_key: str):
+    """DRAM bytes per launch of a kernel, from the committed ncu summary."""
+    p = ROOT / "profiles" / "traffic.json"
+    try:
+        return json.loads(p.read_text()).get(kernel_key)
+    except (OSError, ValueError):
+        return None
+
+
+# ----------------------------------------------------------------------------
+# CPU oracle timing (baseline and reference arm)
+
+
+def oracle_sample_run(host_scene: dict, raw_prepared, pixels: np.ndarray, nthreads: int):
+    from oracle import oracle
+    t0 = time.perf_counter()
+    oracle.focus_scene(host_scene, pixels=pixels, nthreads=nthreads, raw_prepared=raw_prepared)
+    return time.perf_counter() - t0
+
+
+def pick_sample(host_scene, raw_prepared, nthreads, seconds, rng):
+    """Seeded random pixel sample sized for ~`seconds` of CPU work."""
+    from sar_backprojection_gb300 import synth
+    npix = host_scene["xxg1"].size
+    perm = rng.permutation(npix)
+    probe = perm[: max(64, npix // 400)]
+    dt = oracle_sample_run(host_scene, raw_prepared, probe, nthreads)
+    per_px = dt / probe.size
+    n = int(min(npix, max(probe.size, seconds / max(per_px, 1e-9))))
+    pix = np.sort(perm[:n])
+    sint = np.asarray(host_scene["Sint"]).reshape(-1, order="F")[pix].astype(np.int64)
+    mask = np.asarray(host_scene["Mask"]).reshape(-1, order="F")[pix]
+    jj = np.where(sint >= 0, (sint + 1) // 2, -((-sint) // 2)) * 2 + 1
+    work = int(np.where((mask == 1) & (sint != -9999) & (jj > 0), jj, 0).sum())
+    return pix, work
+
+
+def host_scene_of(scene: dict) -> dict:
+    h = dict(scene)
+    raw = scene["RawData"]
+    if hasattr(raw, "detach"):
+        h["RawData"] = raw.detach().cpu()
+    return h
+
+
+# ----------------------------------------------------------------------------
+
+
+def run_reference(args, dist: Dist):
+    """The reference algorithm's CPU implementation on the host cores."""
+    if dist.rank != 0:
+        return
+    import torch
+    from oracle import oracle
+    from sar_backprojection_gb300 import synth
+
+    spec = synth.config_full(args.seed)
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    scene = synth.generate(spec, raw_device=dev)        # input synthesis only
+    host = host_scene_of(scene)
+    raw_prepared = oracle._raw_pulse_major(host["RawData"])
+    cores = len(os.sched_getaffinity(0))
+    rng = np.random.default_rng(1234)
+    per_step = max(0.5, min(3.0, 120.0 / max(args.steps + args.warmup, 1)))
+    pix, work = pick_sample(host, raw_prepared, cores, per_step, rng)
+    for _ in range(args.warmup):
+        oracle_sample_run(host, raw_prepared, pix, cores)
+    times = [oracle_sample_run(host, raw_prepared, pix, cores) for _ in range(args.steps)]
+    total = sum(times)
+    value = work * args.steps / total / 1e9
+    sample = (f"{pix.size} of {host['xxg1'].size} pixels (seeded uniform sample, "
+              f"{work} nominal pixel-pulses) per step")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": DATA,
+        "config": {"workload": WORKLOAD, "precision": "fp64 (reference semantics)",
+                   "implementation": "oracle C restatement of process_point/"
+                                     "FocalizzatoreBpPx, OpenMP over pixels",
+                   "l2": "host run (no GPU)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, dist: Dist):
+    import ctypes as C
+
+    import torch
+
+    from sar_backprojection_gb300 import (FocalizzatoreBpPx, _lib, focus, quality, roofline,
+                                          scene_to_device, synth)
+    from sar_backprojection_gb300.focuser import resolve_tuning
+
+    assert torch.cuda.is_available(), "bench.py needs a CUDA device"
+    dev = torch.device("cuda", dist.local)
+    torch.cuda.set_device(dev)
+    dist.init("nccl")
+    lib = _lib.load()
+
+    tuning = resolve_tuning(None)
+    if args.tuning:
+        vals = [int(v) for v in args.tuning.split(",")]
+        for k, v in zip(("chunk", "tile0", "tile1", "staged"), vals):
+            setattr(tuning, k, v)
+
+    spec = synth.config_full(args.seed + dist.rank)
+    scene = synth.generate(spec, raw_device=str(dev))
+    ds = scene_to_device(*synth.focus_args(scene), device=dev)
+    work = ds.nominal_pixel_pulses()
+    sc = C.byref(ds.struct())
+    tb = C.byref(tuning)
+    ws_bytes = _lib.check(int(lib.sarbp_mixed_workspace_size(sc, tb)))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    out = torch.empty((ds.npix, 2), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    def step(ev0=None, ev1=None):
+        _lib.check(lib.sarbp_mixed_prepare(sc, tb, ws.data_ptr(), ws_bytes, sp))
+        if ev0 is not None:
+            ev0.record(stream)
+        _lib.check(lib.sarbp_focus_mixed_prepared(sc, tb, out.data_ptr(), None, None, None,
+                                                  ws.data_ptr(), ws_bytes, sp))
+        if ev1 is not None:
+            ev1.record(stream)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize(dev)
+    dist.barrier()
+    torch.cuda.synchronize(dev)
+
+    clocks = ClockSampler(device_uuid(dev))
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for k in range(args.steps):
+        step(*ev[k])
+    t_end.record(stream)
+    torch.cuda.synchronize(dev)
+    clock_info = clocks.stop()
+    dist.barrier()
+    elapsed_ms = t_start.elapsed_time(t_end)
+    kernel_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    elapsed_ms = dist.max(elapsed_ms, dev)
+    ms_per_step = elapsed_ms / args.steps
+    value = dist.world * work / (ms_per_step * 1e-3) / 1e9
+    gpu_launches = 2 * args.steps
+
+    # the plain FP64 kernel on the same scene (comparator), and quality
+    mixed_img = out.clone()
+    f64 = focus(ds, "fp64")
+    torch.cuda.synchronize(dev)
+    f_ms = []
+    for _ in range(args.fp64_steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        focus(ds, "fp64", out=f64.image)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        f_ms.append(a.elapsed_time(b))
+    fp64_ms = statistics.mean(f_ms)
+    q = quality.compare(mixed_img.cpu().numpy(), f64.image.cpu().numpy())
+    dm = focus(ds, "mixed", tuning=tuning, diagnostics=True)
+    df = focus(ds, "fp64", diagnostics=True)
+    torch.cuda.synchronize(dev)
+    bins_exact = bool(torch.equal(dm.nvalid, df.nvalid) and torch.equal(dm.checksum, df.checksum))
+    counters = dm.counters.cpu().tolist()
+
+    # roofline of the main kernel
+    rates = (C.c_double * 4)()
+    _lib.check(lib.sarbp_probe_issue_rates(rates, sp))
+    ffma, sfu, dfma, sms = rates[0], rates[1], rates[2], rates[3]
+    peak = roofline.peak_pixel_pulses(ffma, sfu) / 1e9
+    achieved = work / (kernel_ms * 1e-3) / 1e9
+    peak64 = roofline.peak_pixel_pulses_fp64(dfma) / 1e9
+    achieved64 = work / (fp64_ms * 1e-3) / 1e9
+    idx = ds.index.to(torch.int64)
+    s = ds.sint.to(torch.int64)
+    active = (ds.mask == 1) & (ds.sint != -9999)
+    half = (s.abs() + 1) // 2
+    lo = int(torch.clamp((idx - half)[active].min(), min=1))
+    hi = int(torch.clamp((idx + half)[active].max(), max=ds.naz - 2))
+    alg_bytes = roofline.algorithmic_bytes(ds.npix, ds.naz, ds.nra, hi - lo + 1)
+    hbm_peak = measured_peaks().get("hbm_gbs")
+    hbm_achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
+    traffic = profile_traffic("focus_mixed_main:full_4000x250_40001")
+
+    # end to end through the drop-in call, pinned host inputs
+    e2e = None
+    lat = None
+    if args.e2e_steps > 0:
+        host = {}
+        names = ("xxg1", "yyg1", "zzg1", "Mask", "Index", "wgsx", "wgsy", "wgsz")
+        for k in names:
+            a = np.asarray(scene[k])
+            t = torch.from_numpy(np.ascontiguousarray(a.T) if a.ndim == 2 else a)
+            host[k] = (t.pin_memory().t() if a.ndim == 2 else t.pin_memory())
+        a = np.asarray(scene["Sint"])
+        host["Sint"] = torch.from_numpy(np.ascontiguousarray(a.T)).pin_memory().t()
+        raw_pinned = torch.empty((ds.naz, ds.nra), dtype=torch.complex64, pin_memory=True)
+        raw_pinned.copy_(scene["RawData"].t())
+        host["RawData"] = raw_pinned.t()
+        h2d = sum(t.numel() * t.element_size() for t in host.values())
+        d2h = ds.npix * 16
+        argv = (host["xxg1"], host["yyg1"], host["zzg1"], host["Mask"], host["Index"],
+                host["wgsx"], host["wgsy"], host["wgsz"], host["RawData"],
+                float(scene["NearRange"]), float(scene["DeltaRange"]), float(scene["Lambda"]),
+                host["Sint"])
+        for _ in range(2):
+            FocalizzatoreBpPx(*argv, precision="mixed", tuning=tuning, device=dev)
+        torch.cuda.synchronize(dev)
+        dist.barrier()
+        times = []
+        for _ in range(args.e2e_steps):
+            t0 = time.perf_counter()
+            img = FocalizzatoreBpPx(*argv, precision="mixed", tuning=tuning, device=dev)
+            times.append(time.perf_counter() - t0)
+        assert img.shape == (ds.dim0, ds.dim1) and img.dtype == np.complex128
+        gpu_launches += 2 * args.e2e_steps
+        e2e_s = dist.max(statistics.mean(times), dev)
+        e2e = {"value": dist.world * work / e2e_s / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "ms_per_step": 1e3 * e2e_s, "api": "FocalizzatoreBpPx(..., precision='mixed')"}
+        ts = sorted(times)
+        lat = {"p50_ms": 1e3 * float(np.percentile(ts, 50)),
+               "p99_ms": 1e3 * float(np.percentile(ts, 99)),
+               "what": "single-scene drop-in call latency (host inputs to host image)"}
+
+    cpu = None
+    if not args.no_cpu_baseline and dist.rank == 0:
+        from oracle import oracle
+        host_sc = host_scene_of(scene)
+        raw_prepared = oracle._raw_pulse_major(host_sc["RawData"])
+        cores = len(os.sched_getaffinity(0))
+        pix, w_s = pick_sample(host_sc, raw_prepared, cores, args.cpu_seconds,
+                               np.random.default_rng(1234))
+        dt = oracle_sample_run(host_sc, raw_prepared, pix, cores)
+        cpu = {"value": w_s / dt / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{pix.size} of {ds.npix} pixels (seeded uniform), {w_s} pixel-pulses, "
+                         f"{dt:.1f} s"}
+
+    if dist.rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 per pulse + f64 per chunk reference (mixed)", "data": DATA,
+            "config": {"workload": WORKLOAD, "precision": "mixed",
+                       "nominal_pixel_pulses_per_scene": work,
+                       "tuning": tuning.as_dict(),
+                       "l2": "inputs larger than L2 (1.52 GB raw data re-read every step)",
+                       "scenes": f"one per GPU (seed {args.seed}+rank)"},
+            "fp64": {"value": dist.world * work / (fp64_ms * 1e-3) / 1e9, "unit": UNIT,
+                     "ms_per_step": fp64_ms, "steps": args.fp64_steps},
+            "speedup_mixed_vs_fp64": fp64_ms / ms_per_step,
+            "quality": {"vs": "FP64 kernel (bit-exact bins with the oracle)",
+                        "coherence": q["coherence"], "rms_phase_mrad": q["rms_phase_mrad"],
+                        "rel_l2": q["rel_l2"], "bins_bit_exact": bins_exact,
+                        "ambiguous_bins_rederived": counters[_lib.CTR_AMBIGUOUS]},
+            "latency": lat,
+            "roofline": {"bound": "fp32_sfu_issue", "achieved": achieved, "peak": peak,
+                         "unit": UNIT, "frac": achieved / peak, "traffic": traffic,
+                         "kernel_ms": kernel_ms,
+                         "peak_source": "measured in-run by libsarbp probe kernels: "
+                                        f"FP32 FMA {ffma / 1e12:.1f} Tlane/s, SFU "
+                                        f"{sfu / 1e12:.2f} Tops/s -> min(/{roofline.N_FP32}, "
+                                        f"/{roofline.N_SFU})"},
+            "roofline_hbm": {"bound": "hbm", "achieved": hbm_achieved, "peak": hbm_peak,
+                             "unit": "GB/s",
+                             "frac": (hbm_achieved / hbm_peak) if hbm_peak else None,
+                             "traffic": traffic, "algorithmic_bytes": alg_bytes,
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+            "roofline_fp64": {"bound": "fp64_issue", "achieved": achieved64, "peak": peak64,
+                              "unit": UNIT, "frac": achieved64 / peak64,
+                              "peak_source": f"probe FP64 FMA {dfma / 1e12:.2f} Tlane/s "
+                                             f"/{roofline.N_FP64}"},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": gpu_launches,
+            "clocks": clock_info,
+            "sms": int(sms),
+        }
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    if args.impl == "reference":
+        run_reference(args, dist)
+        return
+    run_ours(args, dist)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,171 @@
+/*
+ * sarbp.h -- C ABI of the GB300 SAR time-domain back-projection focuser.
+ *
+ * One shared library (libsarbp.so) with plain-C entry points: plain pointers
+ * and sizes, no C++ types and no exceptions across the boundary.  Every call
+ * returns an int status (SARBP_OK == 0, negative on error) and leaves a
+ * human-readable message for sarbp_last_error() on the calling thread.
+ *
+ * All array pointers are DEVICE pointers (any allocator: PyTorch tensors,
+ * cudaMalloc, ...), and `stream` is a cudaStream_t passed as void* (NULL =
+ * legacy default stream).  Calls are stream-ordered and asynchronous unless
+ * stated otherwise; they are safe to make from several host threads as long
+ * as no two concurrent calls share an output or workspace buffer.
+ *
+ * The call these entry points replace is the reference's focusing function
+ *   FocalizzatoreBpPx(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz,
+ *                     Raw_Data, near_range, dra, lambda_val, Sint)
+ * (sar_focuser_puntual_noui.py:149-284, per-pixel body :9-144) and its GPU
+ * twins FocalizzatoreBpCuPy / FocalizzatoreBpCuPy_Batched
+ * (gpu_small_dataset.py:113-223, :229-362, kernel :9-108) and the chunked
+ * driver's kernel (main_gpu.py:60-155).
+ */
+#ifndef SARBP_H
+#define SARBP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SARBP_API __attribute__((visibility("default")))
+
+/* Status codes. */
+#define SARBP_OK            0
+#define SARBP_EINVAL       -1   /* bad argument (NULL pointer, bad size, ...) */
+#define SARBP_EWORKSPACE   -2   /* workspace missing or too small */
+#define SARBP_ECUDA        -3   /* CUDA runtime error (message has details) */
+#define SARBP_ETIMEOUT     -4   /* a bounded device wait gave up */
+#define SARBP_ERANGE       -5   /* size beyond a documented limit */
+#define SARBP_EDEVICE      -6   /* device is not a GB300-class sm_103 GPU */
+
+/*
+ * One focusing scene: the reference's 13 positional arguments
+ * (sar_focuser_puntual_noui.py:149, argument order xxg1, yyg1, zzg1, mask,
+ * index, wgsx, wgsy, wgsz, Raw_Data, near_range, dra, lambda_val, Sint).
+ *
+ * DEM grid arrays hold dim0*dim1 pixels flattened in column-major (Fortran)
+ * order, pixel ii = i0 + dim0*i1, exactly as the reference flattens them
+ * (sar_focuser_puntual_noui.py:183-188).  The output image uses the same
+ * order.
+ *
+ * Raw data are complex64 stored as interleaved float pairs (re, im), range
+ * fastest: sample (range bin r, pulse a) is at raw[2*(a*raw_pitch + r)].  With
+ * raw_pitch == nra this is the reference's column-major (Nra, Naz) complex64
+ * RawData array as read from RawData_Cmplx_<Nra>x<Naz>.dat.  raw_pitch may be
+ * larger (padded rows); the mixed-precision path wants raw + 2*raw_pitch
+ * floats to be 16-byte aligned, i.e. raw 16-byte aligned and raw_pitch even.
+ */
+typedef struct sarbp_scene {
+    int64_t dim0, dim1;                       /* DEM grid shape (xxg1.shape) */
+    const double  *dem_x, *dem_y, *dem_z;     /* xxg1, yyg1, zzg1 [dim0*dim1] */
+    const uint8_t *mask;                      /* Mask_Byte: 1 = focus        */
+    const int32_t *index;                     /* Index_Long: aperture centre */
+    const int32_t *sint;                      /* Sint_Long: aperture length, -9999 = none */
+    const double  *traj_x, *traj_y, *traj_z;  /* wgsx, wgsy, wgsz [>= naz]   */
+    const float   *raw;                       /* Raw_Data, see above         */
+    int64_t nra, naz, raw_pitch;              /* Raw_Data.shape, row pitch   */
+    double near_range, delta_range, lambda;   /* near_range, dra, lambda_val */
+} sarbp_scene;
+
+/*
+ * Tuning of the mixed-precision kernel.  Zero-initialised fields take the
+ * library default; sarbp_default_tuning() fills the defaults explicitly.
+ */
+typedef struct sarbp_tuning {
+    int32_t chunk;        /* pulses per chunk: 32 or 64                       */
+    int32_t tile0;        /* pixel-tile extent along dim0 (power of two)      */
+    int32_t tile1;        /* pixel-tile extent along dim1                     */
+    int32_t staged;       /* 1: TMA-staged shared-memory raw window, 0: L1/L2 gathers */
+    int32_t reserved[4];
+} sarbp_tuning;
+
+/* Device counters written by the mixed kernel when `counters` is non-NULL. */
+#define SARBP_CTR_AMBIGUOUS   0   /* range bins re-derived in FP64 (near .5 ties) */
+#define SARBP_CTR_WINDOW_MISS 1   /* staged-window misses served from L2         */
+#define SARBP_CTR_CHUNKS      2   /* pixel x chunk work items processed          */
+#define SARBP_CTR_TIMEOUTS    3   /* bounded waits that gave up                  */
+#define SARBP_NUM_COUNTERS    8
+
+/* Library version (major*10000 + minor*100 + patch). */
+SARBP_API int sarbp_version(void);
+
+/* Last error message on the calling thread ("" if none). */
+SARBP_API const char *sarbp_last_error(void);
+
+/* Fill `t` with the library defaults. */
+SARBP_API int sarbp_default_tuning(sarbp_tuning *t);
+
+/*
+ * Plain FP64 focusing, one thread per pixel, with the reference CPU path's
+ * exact semantics: nearest range bin with round-half-to-even, strict pulse
+ * bounds 0 < a < Naz-1, bins 0 <= bin < Nra-1, float32-literal pi, beta*R^2
+ * phase term, division by the contributor count.
+ * Replaces process_point + the pixel loop of FocalizzatoreBpPx
+ * (sar_focuser_puntual_noui.py:9-144, :232-241) and the CuPy kernel
+ * process_point_kernel (gpu_small_dataset.py:9-108), whose rounding
+ * (half away from zero) it does NOT copy.
+ *
+ * out       complex128 image, dim0*dim1 (re, im) double pairs, column-major.
+ * nvalid    optional (NULL): per-pixel contributor count.
+ * checksum  optional (NULL): per-pixel sum of mix64(pulse, bin) over the
+ *           contributing pulses (bit-exact range-bin selection check).
+ */
+SARBP_API int sarbp_focus_fp64(const sarbp_scene *scene, double *out,
+                               int32_t *nvalid, uint64_t *checksum,
+                               void *stream);
+
+/*
+ * Bytes of device workspace the mixed-precision path needs for `scene`
+ * (>= 0), or a negative status.  The workspace holds the per-pulse chunk
+ * table, per-tile plans and a status block; it can be reused across calls
+ * on the same stream.
+ */
+SARBP_API int64_t sarbp_mixed_workspace_size(const sarbp_scene *scene,
+                                             const sarbp_tuning *tuning);
+
+/*
+ * Mixed-precision focusing: FP64 slant range and phase wrap at each pulse-
+ * chunk reference, FP32 differential range / phase / accumulation per pulse,
+ * compensated (Kahan) summation across chunks, range bins that match the
+ * FP64 path bit-exactly (ambiguous ties are re-derived in FP64).
+ * Same outputs as sarbp_focus_fp64.  `counters` (optional, device,
+ * SARBP_NUM_COUNTERS uint64) is incremented, not cleared.
+ * Replaces the same reference code as sarbp_focus_fp64.
+ */
+SARBP_API int sarbp_focus_mixed(const sarbp_scene *scene,
+                                const sarbp_tuning *tuning,
+                                double *out, int32_t *nvalid,
+                                uint64_t *checksum, uint64_t *counters,
+                                void *workspace, size_t workspace_bytes,
+                                void *stream);
+
+/*
+ * The two halves of sarbp_focus_mixed, for callers that keep a scene
+ * resident and focus it repeatedly (serving, benchmarking): _prepare builds
+ * the per-pulse chunk tables in the workspace (they depend on the trajectory
+ * only), _prepared runs the focusing kernel on a prepared workspace.
+ * sarbp_focus_mixed == sarbp_mixed_prepare + sarbp_focus_mixed_prepared.
+ * Same reference counterpart as sarbp_focus_fp64.
+ */
+SARBP_API int sarbp_mixed_prepare(const sarbp_scene *scene, const sarbp_tuning *tuning,
+                                  void *workspace, size_t workspace_bytes, void *stream);
+SARBP_API int sarbp_focus_mixed_prepared(const sarbp_scene *scene, const sarbp_tuning *tuning,
+                                         double *out, int32_t *nvalid, uint64_t *checksum,
+                                         uint64_t *counters, void *workspace,
+                                         size_t workspace_bytes, void *stream);
+
+/*
+ * Measurement helper (no counterpart in the reference, which publishes no
+ * roofline): measures this device's issue rates with probe kernels on
+ * `stream` and returns them in rates[0..3] = FP32 FMA lanes/s, SFU sin
+ * evaluations/s, FP64 FMA lanes/s, SM count.  Synchronises the stream.
+ */
+SARBP_API int sarbp_probe_issue_rates(double *rates, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SARBP_H */

@@ -1,0 +1,203 @@
+// capi.cu -- the extern "C" boundary: argument validation, scene constants,
+// status codes and the per-thread error message.  No exception crosses it.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+
+#include "sarbp_internal.cuh"
+
+namespace sarbp {
+
+static thread_local char g_last_error[512];
+
+void set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+}
+
+int cuda_status(cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess) return SARBP_OK;
+    set_error("%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+    return SARBP_ECUDA;
+}
+
+// Validate a scene and derive the kernel constants with the reference's
+// evaluation order (sar_focuser_puntual_noui.py:29, :105).
+bool build_params(const sarbp_scene *s, SceneParams *p)
+{
+    if (!s) {
+        set_error("scene is NULL");
+        return false;
+    }
+    if (s->dim0 <= 0 || s->dim1 <= 0) {
+        set_error("DEM grid shape (%lld, %lld) must be positive", (long long)s->dim0,
+                  (long long)s->dim1);
+        return false;
+    }
+    if (!s->dem_x || !s->dem_y || !s->dem_z || !s->mask || !s->index || !s->sint ||
+        !s->traj_x || !s->traj_y || !s->traj_z || !s->raw) {
+        set_error("a scene array pointer is NULL");
+        return false;
+    }
+    if (s->nra <= 0 || s->naz <= 0 || s->nra > 0x7fffffffLL || s->naz > 0x3fffffffLL) {
+        set_error("Raw_Data shape (%lld, %lld) is outside 1..2^31-1 x 1..2^30-1",
+                  (long long)s->nra, (long long)s->naz);
+        return false;
+    }
+    if (s->raw_pitch < s->nra) {
+        set_error("raw_pitch %lld is smaller than nra %lld", (long long)s->raw_pitch,
+                  (long long)s->nra);
+        return false;
+    }
+    if (!(s->delta_range != 0.0) || !(s->lambda != 0.0)) {
+        set_error("delta_range and lambda must be non-zero");
+        return false;
+    }
+    p->dim0 = s->dim0;
+    p->dim1 = s->dim1;
+    p->npix = s->dim0 * s->dim1;
+    p->x = s->dem_x;
+    p->y = s->dem_y;
+    p->z = s->dem_z;
+    p->mask = s->mask;
+    p->index = s->index;
+    p->sint = s->sint;
+    p->tx = s->traj_x;
+    p->ty = s->traj_y;
+    p->tz = s->traj_z;
+    p->raw = reinterpret_cast<const float2 *>(s->raw);
+    p->nra = s->nra;
+    p->naz = s->naz;
+    p->pitch = s->raw_pitch;
+    p->near_range = s->near_range;
+    p->dra = s->delta_range;
+    p->lambda = s->lambda;
+    volatile double four = 4.0, pi = kPiF32, alfa = kAlfa, c = kC;
+    p->beta = four * pi * alfa / (c * c);
+    p->k4pl = -four * pi / s->lambda;
+    p->inv_dra = 1.0 / s->delta_range;
+    return true;
+}
+
+static bool valid_tuning(sarbp_tuning *t)
+{
+    if (t->chunk == 0) t->chunk = 64;
+    if (t->tile0 == 0 && t->tile1 == 0) {
+        t->tile0 = 32;
+        t->tile1 = 8;
+    }
+    if (t->chunk != 32 && t->chunk != 64) {
+        set_error("tuning.chunk must be 32 or 64 (got %d)", t->chunk);
+        return false;
+    }
+    return true;
+}
+
+}  // namespace sarbp
+
+using namespace sarbp;
+
+extern "C" {
+
+SARBP_API int sarbp_version(void) { return 100; }
+
+SARBP_API const char *sarbp_last_error(void) { return g_last_error; }
+
+SARBP_API int sarbp_default_tuning(sarbp_tuning *t)
+{
+    if (!t) {
+        set_error("tuning is NULL");
+        return SARBP_EINVAL;
+    }
+    memset(t, 0, sizeof(*t));
+    valid_tuning(t);
+    return SARBP_OK;
+}
+
+SARBP_API int sarbp_focus_fp64(const sarbp_scene *scene, double *out, int32_t *nvalid,
+                               uint64_t *checksum, void *stream)
+{
+    g_last_error[0] = 0;
+    SceneParams P;
+    if (!build_params(scene, &P)) return SARBP_EINVAL;
+    if (!out) {
+        set_error("sarbp_focus_fp64: out is NULL");
+        return SARBP_EINVAL;
+    }
+    return launch_focus_fp64(P, out, nvalid, checksum, static_cast<cudaStream_t>(stream));
+}
+
+SARBP_API int64_t sarbp_mixed_workspace_size(const sarbp_scene *scene, const sarbp_tuning *tuning)
+{
+    g_last_error[0] = 0;
+    SceneParams P;
+    if (!build_params(scene, &P)) return SARBP_EINVAL;
+    sarbp_tuning T{};
+    if (tuning) T = *tuning;
+    if (!valid_tuning(&T)) return SARBP_EINVAL;
+    return (int64_t)mixed_layout(P.naz, T.chunk).total;
+}
+
+static int mixed_args(const sarbp_scene *scene, const sarbp_tuning *tuning, SceneParams *P,
+                      sarbp_tuning *T)
+{
+    g_last_error[0] = 0;
+    if (!build_params(scene, P)) return SARBP_EINVAL;
+    *T = sarbp_tuning{};
+    if (tuning) *T = *tuning;
+    if (!valid_tuning(T)) return SARBP_EINVAL;
+    return SARBP_OK;
+}
+
+SARBP_API int sarbp_mixed_prepare(const sarbp_scene *scene, const sarbp_tuning *tuning,
+                                  void *workspace, size_t workspace_bytes, void *stream)
+{
+    SceneParams P;
+    sarbp_tuning T;
+    int rc = mixed_args(scene, tuning, &P, &T);
+    if (rc) return rc;
+    return launch_mixed_prepare(P, T, workspace, workspace_bytes,
+                                static_cast<cudaStream_t>(stream));
+}
+
+SARBP_API int sarbp_focus_mixed_prepared(const sarbp_scene *scene, const sarbp_tuning *tuning,
+                                         double *out, int32_t *nvalid, uint64_t *checksum,
+                                         uint64_t *counters, void *workspace,
+                                         size_t workspace_bytes, void *stream)
+{
+    SceneParams P;
+    sarbp_tuning T;
+    int rc = mixed_args(scene, tuning, &P, &T);
+    if (rc) return rc;
+    if (!out) {
+        set_error("sarbp_focus_mixed: out is NULL");
+        return SARBP_EINVAL;
+    }
+    return launch_mixed_main(P, T, workspace, workspace_bytes, out, nvalid, checksum, counters,
+                             static_cast<cudaStream_t>(stream));
+}
+
+SARBP_API int sarbp_focus_mixed(const sarbp_scene *scene, const sarbp_tuning *tuning, double *out,
+                                int32_t *nvalid, uint64_t *checksum, uint64_t *counters,
+                                void *workspace, size_t workspace_bytes, void *stream)
+{
+    SceneParams P;
+    sarbp_tuning T;
+    int rc = mixed_args(scene, tuning, &P, &T);
+    if (rc) return rc;
+    if (!out) {
+        set_error("sarbp_focus_mixed: out is NULL");
+        return SARBP_EINVAL;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    rc = launch_mixed_prepare(P, T, workspace, workspace_bytes, s);
+    if (rc) return rc;
+    return launch_mixed_main(P, T, workspace, workspace_bytes, out, nvalid, checksum, counters,
+                             s);
+}
+
+}  // extern "C"

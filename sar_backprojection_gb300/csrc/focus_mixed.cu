@@ -1,0 +1,285 @@
+// focus_mixed.cu -- mixed-precision pixel-tiled back-projection.
+//
+// Work decomposition: one CTA per pixel tile (tile0 x tile1 pixels of the
+// column-major DEM grid, one thread per pixel); the union of the tile's
+// apertures is walked in pulse chunks aligned to multiples of `chunk`.
+// Precision plan: mixed_common.cuh.  This file holds the chunk-table prep
+// kernel, the L1/L2-gather main kernel and the launch logic; the TMA-staged
+// main kernel lives in focus_staged.cu.
+#include <climits>
+#include <cstdio>
+
+#include "mixed_common.cuh"
+
+namespace sarbp {
+
+static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+MixedLayout mixed_layout(int64_t naz, int chunk)
+{
+    MixedLayout L{};
+    size_t off = align256(sizeof(StatusBlock));
+    L.ptab = off;
+    off = align256(off + sizeof(float4) * (size_t)naz);
+    L.ctab = off;
+    const int64_t nchunks = (naz + chunk - 1) / chunk;
+    off = align256(off + sizeof(float4) * (size_t)nchunks);
+    L.total = off;
+    return L;
+}
+
+__device__ __forceinline__ int64_t chunk_ref(int64_t c, int chunk, int64_t naz)
+{
+    const int64_t k0 = c * chunk + chunk / 2;
+    return k0 < naz - 1 ? k0 : naz - 1;
+}
+
+// Per-pulse chunk table and per-chunk bounds; one warp per chunk.
+__global__ void chunk_table_kernel(const SceneParams P, int chunk, float4 *__restrict__ ptab,
+                                   float4 *__restrict__ ctab, int64_t nchunks)
+{
+    const int64_t c = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (c >= nchunks) return;
+    const int64_t k0 = chunk_ref(c, chunk, P.naz);
+    const double x0 = P.tx[k0], y0 = P.ty[k0], z0 = P.tz[k0];
+    float mx = 0.f, my = 0.f, mz = 0.f, m2 = 0.f;
+    for (int j = lane; j < chunk; j += 32) {
+        const int64_t k = c * chunk + j;
+        if (k >= P.naz) break;
+        const double ex = P.tx[k] - x0, ey = P.ty[k] - y0, ez = P.tz[k] - z0;
+        const double e2 = ex * ex + ey * ey + ez * ez;
+        const float4 e = make_float4((float)ex, (float)ey, (float)ez, (float)e2);
+        ptab[k] = e;
+        // Bounds rounded up by one part in 2^20 so they hold for the FP32 values.
+        mx = fmaxf(mx, fabsf(e.x) * 1.000001f);
+        my = fmaxf(my, fabsf(e.y) * 1.000001f);
+        mz = fmaxf(mz, fabsf(e.z) * 1.000001f);
+        m2 = fmaxf(m2, e.w * 1.000001f);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        my = fmaxf(my, __shfl_xor_sync(0xffffffffu, my, o));
+        mz = fmaxf(mz, __shfl_xor_sync(0xffffffffu, mz, o));
+        m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+    }
+    if (lane == 0) ctab[c] = make_float4(mx, my, mz, m2);
+}
+
+// Main kernel, raw samples gathered through L1/L2.
+template <int CHUNK, int T0, int T1, bool kChecksum>
+__global__ void __launch_bounds__(T0 *T1)
+focus_mixed_gather_kernel(const SceneParams P, const float4 *__restrict__ ptab,
+                          const float4 *__restrict__ ctab, int64_t ntile0,
+                          double2 *__restrict__ out, int32_t *__restrict__ nvalid,
+                          uint64_t *__restrict__ checksum, unsigned long long *__restrict__ counters)
+{
+    __shared__ long long s_lo, s_hi;
+    const int t = threadIdx.x;
+    const int64_t tile = blockIdx.x;
+    const int64_t i0 = (tile % ntile0) * T0 + (t % T0);
+    const int64_t i1 = (tile / ntile0) * T1 + (t / T0);
+    const bool inside = i0 < P.dim0 && i1 < P.dim1;
+    const int64_t ii = inside ? i0 + P.dim0 * i1 : 0;
+    int64_t lo = 0, hi = -1;
+    const bool active =
+        inside && pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi);
+
+    if (t == 0) {
+        s_lo = LLONG_MAX;
+        s_hi = -1;
+    }
+    __syncthreads();
+    if (active) {
+        atomicMin(&s_lo, (long long)lo);
+        atomicMax(&s_hi, (long long)hi);
+    }
+    __syncthreads();
+    const int64_t tlo = s_lo, thi = s_hi;
+
+    double px = 0.0, py = 0.0, pz = 0.0;
+    if (active) {
+        px = P.x[ii];
+        py = P.y[ii];
+        pz = P.z[ii];
+    }
+    float acc_re = 0.f, acc_im = 0.f, cmp_re = 0.f, cmp_im = 0.f;
+    int n = 0;
+    uint64_t cs = 0;
+    unsigned ambiguous = 0, chunks = 0;
+    const float inv_dra_f = (float)P.inv_dra;
+    const float beta_f = (float)P.beta;
+    const unsigned nra_m1 = (unsigned)(P.nra - 1);
+
+    if (thi >= 0) {
+        for (int64_t c = tlo / CHUNK; c <= thi / CHUNK; ++c) {
+            const int64_t K = c * CHUNK;
+            const int64_t kmin = lo > K ? lo : K;
+            const int64_t kmax = hi < K + CHUNK - 1 ? hi : K + CHUNK - 1;
+            if (!active || kmin > kmax) continue;
+            ++chunks;
+            ChunkSetup S;
+            chunk_setup(P, px, py, pz, chunk_ref(c, CHUNK, P.naz), __ldg(ctab + c), S);
+            if (S.exact) {
+                double sre = 0.0, sim = 0.0;
+                for (int64_t a = kmin; a <= kmax; ++a) {
+                    int64_t bin;
+                    double tre, tim;
+                    if (exact_term(P, px, py, pz, a, &bin, &tre, &tim)) {
+                        sre += tre;
+                        sim += tim;
+                        ++n;
+                        if (kChecksum) cs += mix64(a, bin);
+                    }
+                }
+                kahan_add(acc_re, cmp_re, (float)sre);
+                kahan_add(acc_im, cmp_im, (float)sim);
+                continue;
+            }
+            float sre = 0.f, sim = 0.f;
+            const float2 *row = P.raw + kmin * P.pitch;
+            for (int64_t k = kmin; k <= kmax; ++k, row += P.pitch) {
+                const float4 e = __ldg(ptab + k);
+                const float D = fmaf(S.mx, e.x, fmaf(S.my, e.y, fmaf(S.mz, e.z, e.w)));
+                const float dR = D * fmaf(fmaf(S.c3, D, S.c2), D, S.c1);
+                const float g = fmaf(dR, inv_dra_f, S.g0);
+                const float rnd = __fadd_rn(g, 12582912.0f);
+                int bin = S.n0 + (__float_as_int(rnd) - 0x4B400000);
+                const float fr = __fsub_rn(g, __fsub_rn(rnd, 12582912.0f));
+                if (fabsf(fr) > kAmbiguity) {
+                    double r2, r;
+                    const int64_t eb = exact_bin(px, py, pz, __ldg(P.tx + k), __ldg(P.ty + k),
+                                                 __ldg(P.tz + k), P.near_range, P.dra, P.nra,
+                                                 &r2, &r);
+                    bin = (int)eb;
+                    ++ambiguous;
+                }
+                const bool ok = (unsigned)bin < nra_m1;
+                float2 v = make_float2(0.f, 0.f);
+                if (ok) v = __ldg(row + bin);
+                const float ph = dR * fmaf(beta_f, dR, S.a);
+                float sn, cn;
+                __sincosf(ph, &sn, &cn);
+                const float tre = fmaf(v.x, cn, v.y * sn);
+                const float tim = fmaf(v.y, cn, -(v.x * sn));
+                const float w = S.r0sq + D;
+                sre = fmaf(w, tre, sre);
+                sim = fmaf(w, tim, sim);
+                n += ok ? 1 : 0;
+                if (kChecksum && ok) cs += mix64(k, bin);
+            }
+            // chunk sum * exp(-j*phi0)
+            const float rre = fmaf(sre, S.w0re, -(sim * S.w0im));
+            const float rim = fmaf(sre, S.w0im, sim * S.w0re);
+            kahan_add(acc_re, cmp_re, rre);
+            kahan_add(acc_im, cmp_im, rim);
+        }
+    }
+
+    if (inside) {
+        double2 res = make_double2(0.0, 0.0);
+        if (n > 0) {
+            const double inv = 1.0 / (double)n;
+            res = make_double2(((double)acc_re - (double)cmp_re) * inv,
+                               ((double)acc_im - (double)cmp_im) * inv);
+        }
+        out[ii] = res;
+        if (nvalid) nvalid[ii] = n;
+        if (kChecksum) checksum[ii] = cs;
+    }
+    if (counters) {
+        for (int o = 16; o > 0; o >>= 1) {
+            ambiguous += __shfl_xor_sync(0xffffffffu, ambiguous, o);
+            chunks += __shfl_xor_sync(0xffffffffu, chunks, o);
+        }
+        if ((t & 31) == 0) {
+            if (ambiguous) atomicAdd(counters + SARBP_CTR_AMBIGUOUS, (unsigned long long)ambiguous);
+            if (chunks) atomicAdd(counters + SARBP_CTR_CHUNKS, (unsigned long long)chunks);
+        }
+    }
+}
+
+template <int CHUNK, int T0, int T1>
+static int launch_gather(const SceneParams &P, const MixedLayout &L, char *ws, double *out,
+                         int32_t *nvalid, uint64_t *checksum, uint64_t *counters,
+                         cudaStream_t stream)
+{
+    const int64_t nt0 = (P.dim0 + T0 - 1) / T0, nt1 = (P.dim1 + T1 - 1) / T1;
+    const int64_t tiles = nt0 * nt1;
+    if (tiles > 0x7fffffffLL) {
+        set_error("sarbp_focus_mixed: %lld tiles exceed the launch limit", (long long)tiles);
+        return SARBP_ERANGE;
+    }
+    auto *ptab = reinterpret_cast<const float4 *>(ws + L.ptab);
+    auto *ctab = reinterpret_cast<const float4 *>(ws + L.ctab);
+    auto *ctr = reinterpret_cast<unsigned long long *>(counters);
+    if (checksum)
+        focus_mixed_gather_kernel<CHUNK, T0, T1, true><<<(unsigned)tiles, T0 * T1, 0, stream>>>(
+            P, ptab, ctab, nt0, reinterpret_cast<double2 *>(out), nvalid, checksum, ctr);
+    else
+        focus_mixed_gather_kernel<CHUNK, T0, T1, false><<<(unsigned)tiles, T0 * T1, 0, stream>>>(
+            P, ptab, ctab, nt0, reinterpret_cast<double2 *>(out), nvalid, nullptr, ctr);
+    return cuda_status(cudaGetLastError(), "focus_mixed_gather launch");
+}
+
+int launch_chunk_table(const SceneParams &P, int chunk, char *ws, const MixedLayout &L,
+                       cudaStream_t stream)
+{
+    const int64_t nchunks = (P.naz + chunk - 1) / chunk;
+    const int warps = 8;
+    const int64_t blocks = (nchunks + warps - 1) / warps;
+    chunk_table_kernel<<<(unsigned)blocks, warps * 32, 0, stream>>>(
+        P, chunk, reinterpret_cast<float4 *>(ws + L.ptab), reinterpret_cast<float4 *>(ws + L.ctab),
+        nchunks);
+    return cuda_status(cudaGetLastError(), "chunk_table launch");
+}
+
+static int check_workspace(const MixedLayout &L, void *workspace, size_t ws_bytes)
+{
+    if (!workspace || ws_bytes < L.total) {
+        set_error("sarbp mixed path: workspace of %zu bytes is smaller than the %zu required",
+                  ws_bytes, L.total);
+        return SARBP_EWORKSPACE;
+    }
+    return SARBP_OK;
+}
+
+int launch_mixed_prepare(const SceneParams &P, const sarbp_tuning &T, void *workspace,
+                         size_t ws_bytes, cudaStream_t stream)
+{
+    const MixedLayout L = mixed_layout(P.naz, T.chunk);
+    int rc = check_workspace(L, workspace, ws_bytes);
+    if (rc) return rc;
+    return launch_chunk_table(P, T.chunk, static_cast<char *>(workspace), L, stream);
+}
+
+int launch_mixed_main(const SceneParams &P, const sarbp_tuning &T, void *workspace,
+                      size_t ws_bytes, double *out, int32_t *nvalid, uint64_t *checksum,
+                      uint64_t *counters, cudaStream_t stream)
+{
+    const MixedLayout L = mixed_layout(P.naz, T.chunk);
+    int rc = check_workspace(L, workspace, ws_bytes);
+    if (rc) return rc;
+    char *ws = static_cast<char *>(workspace);
+    const int key = T.chunk * 1000000 + T.tile0 * 1000 + T.tile1;
+    switch (key) {
+        case 32 * 1000000 + 32 * 1000 + 8:
+            return launch_gather<32, 32, 8>(P, L, ws, out, nvalid, checksum, counters, stream);
+        case 64 * 1000000 + 32 * 1000 + 8:
+            return launch_gather<64, 32, 8>(P, L, ws, out, nvalid, checksum, counters, stream);
+        case 32 * 1000000 + 64 * 1000 + 4:
+            return launch_gather<32, 64, 4>(P, L, ws, out, nvalid, checksum, counters, stream);
+        case 64 * 1000000 + 64 * 1000 + 4:
+            return launch_gather<64, 64, 4>(P, L, ws, out, nvalid, checksum, counters, stream);
+        case 32 * 1000000 + 16 * 1000 + 16:
+            return launch_gather<32, 16, 16>(P, L, ws, out, nvalid, checksum, counters, stream);
+        case 64 * 1000000 + 16 * 1000 + 16:
+            return launch_gather<64, 16, 16>(P, L, ws, out, nvalid, checksum, counters, stream);
+        default:
+            set_error("sarbp mixed path: unsupported tuning chunk=%d tile=%dx%d", T.chunk,
+                      T.tile0, T.tile1);
+            return SARBP_EINVAL;
+    }
+}
+
+}  // namespace sarbp

@@ -1,0 +1,119 @@
+// sarbp_internal.cuh -- shared device-side definitions of the focuser kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/sarbp.h"
+
+namespace sarbp {
+
+// Physical constants of the reference (sar_focuser_puntual_noui.py:24-29):
+// speed of light, chirp rate and pi as the float32 literal 3.14159274...
+constexpr double kC = 2.9979246e8;
+constexpr double kAlfa = 3.335987619777693e11;
+constexpr double kPiF32 = 3.141592741012573242;
+
+// Scene constants derived once on the host with the reference's evaluation
+// order, passed to every kernel by value.
+struct SceneParams {
+    int64_t dim0, dim1, npix;
+    const double *x, *y, *z;
+    const uint8_t *mask;
+    const int32_t *index, *sint;
+    const double *tx, *ty, *tz;
+    const float2 *raw;       // sample (r, a) at raw[a*pitch + r]
+    int64_t nra, naz, pitch;
+    double near_range, dra, lambda;
+    double beta;             // 4*pi*alfa/(c*c)                    (:29)
+    double k4pl;             // (-4*pi)/lambda                     (:105)
+    double inv_dra;          // 1/dra (reference-range estimate only)
+};
+
+// Aperture of one pixel, clamped to the kept pulses 0 < a < naz-1
+// (sar_focuser_puntual_noui.py:46-55).  Returns false when nothing is kept
+// or the pixel is masked (:35-42).
+__host__ __device__ inline bool pixel_aperture(uint8_t mask, int32_t sint, int32_t index,
+                                               int64_t naz, int64_t *lo, int64_t *hi)
+{
+    if (mask != 1 || sint == -9999) return false;
+    // jj_size = ceil(s/2)*2 + 1 ; offset = ceil(|s|/2), both on integers.
+    const int64_t s = sint;
+    const int64_t half_up = (s >= 0) ? (s + 1) / 2 : -((-s) / 2);   // ceil(s/2)
+    const int64_t jj_size = half_up * 2 + 1;
+    const int64_t off = (s >= 0) ? (s + 1) / 2 : ((-s) + 1) / 2;    // ceil(|s|/2)
+    if (jj_size <= 0) return false;
+    const int64_t a0 = (int64_t)index - off;
+    int64_t l = a0 > 1 ? a0 : 1;
+    int64_t h = a0 + jj_size - 1;
+    if (h > naz - 2) h = naz - 2;
+    *lo = l;
+    *hi = h;
+    return l <= h;
+}
+
+// SplitMix64 finaliser of (pulse << 32 | bin): per-pixel checksum term of
+// the contributing (pulse, range-bin) pairs.
+__host__ __device__ inline uint64_t mix64(int64_t pulse, int64_t bin)
+{
+    uint64_t z = ((uint64_t)pulse << 32) | (uint64_t)(uint32_t)bin;
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// Exact FP64 range bin of pixel p at pulse a with the reference's rounding
+// sequence (no fused multiply-add): sar_focuser_puntual_noui.py:71-95.
+// Returns -1 when the bin is outside 0 <= bin < nra-1.
+__device__ inline int64_t exact_bin(double px, double py, double pz,
+                                    double tx, double ty, double tz,
+                                    double near_range, double dra, int64_t nra,
+                                    double *r2_out, double *r_out)
+{
+    const double xc = __dsub_rn(px, tx);
+    const double yc = __dsub_rn(py, ty);
+    const double zc = __dsub_rn(pz, tz);
+    const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(xc, xc), __dmul_rn(yc, yc)),
+                                __dmul_rn(zc, zc));
+    const double r = __dsqrt_rn(r2);
+    const double f = __ddiv_rn(__dsub_rn(r, near_range), dra);
+    const double fb = rint(f);
+    *r2_out = r2;
+    *r_out = r;
+    if (!(fb < (double)(nra - 1) && fb >= 0.0)) return -1;
+    return (int64_t)fb;
+}
+
+// Device status block at the head of every workspace.
+struct StatusBlock {
+    unsigned int error;      // non-zero: a bounded wait gave up
+    unsigned int where;      // tag of the wait that gave up
+    unsigned int pad[62];
+};
+
+}  // namespace sarbp
+
+// Host-side helpers shared by the translation units (defined in capi.cu).
+namespace sarbp {
+void set_error(const char *fmt, ...);
+bool build_params(const sarbp_scene *s, SceneParams *p);
+int cuda_status(cudaError_t e, const char *what);
+
+// Mixed-path workspace layout (offsets 256-byte aligned).
+struct MixedLayout {
+    size_t status;   // StatusBlock
+    size_t ptab;     // float4[naz]: e = t(k) - t(k0), |e|^2
+    size_t ctab;     // float4[nchunks]: max |e_x|, |e_y|, |e_z|, |e|^2
+    size_t total;
+};
+MixedLayout mixed_layout(int64_t naz, int chunk);
+
+int launch_focus_fp64(const SceneParams &P, double *out, int32_t *nvalid, uint64_t *checksum,
+                      cudaStream_t stream);
+int launch_mixed_prepare(const SceneParams &P, const sarbp_tuning &T, void *workspace,
+                         size_t ws_bytes, cudaStream_t stream);
+int launch_mixed_main(const SceneParams &P, const sarbp_tuning &T, void *workspace,
+                      size_t ws_bytes, double *out, int32_t *nvalid, uint64_t *checksum,
+                      uint64_t *counters, cudaStream_t stream);
+}  // namespace sarbp

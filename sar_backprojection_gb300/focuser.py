@@ -1,0 +1,135 @@
+"""Focusing calls: the drop-in for the reference's focusing functions.
+
+``FocalizzatoreBpPx`` keeps the reference's 13 positional arguments, their
+meaning and dtype coercions, its ValueErrors and its return value (a fresh
+complex128 array of xxg1's shape) -- sar_focuser_puntual_noui.py:149-284.
+``FocalizzatoreBpCuPy`` and ``FocalizzatoreBpCuPy_Batched`` are the same call
+under the GPU scripts' names (gpu_small_dataset.py:113, :229).  Focusing runs
+on the GPU through libsarbp.so; there is no CPU path.
+
+Keyword-only extras: ``precision`` ("fp64", the reference semantics exactly,
+or "mixed", the mixed-precision kernel), ``tuning`` and ``device``.  The
+reference's progress prints and its ``focalizador_px_checkpoint.npz`` file are
+not reproduced: a full scene focuses in milliseconds on one GB300, so the
+checkpoint has nothing to resume (long scenes use ``large_scene``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from .scene import DeviceScene, scene_to_device
+
+PRECISIONS = ("fp64", "mixed")
+
+
+@dataclass
+class FocusResult:
+    """Device outputs of one focusing call."""
+
+    image: torch.Tensor                    # (npix, 2) float64, column-major pixels
+    nvalid: torch.Tensor | None = None     # (npix,) int32 contributor counts
+    checksum: torch.Tensor | None = None   # (npix,) int64 (bit pattern of uint64)
+    counters: torch.Tensor | None = None   # (NUM_COUNTERS,) int64
+
+    def to_numpy(self, dim0: int, dim1: int) -> np.ndarray:
+        """complex128 image of shape (dim0, dim1), as the reference returns it."""
+        flat = self.image.cpu().numpy().view(np.complex128).reshape(-1)
+        return np.reshape(flat, (dim0, dim1), order="F")
+
+
+def _stream_ptr(device: torch.device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def resolve_tuning(tuning) -> _lib.Tuning:
+    t = _lib.default_tuning()
+    if tuning is None:
+        return t
+    if isinstance(tuning, _lib.Tuning):
+        return tuning
+    for k, v in dict(tuning).items():
+        setattr(t, k, int(v))
+    return t
+
+
+def workspace_bytes(scene: DeviceScene, tuning=None) -> int:
+    t = resolve_tuning(tuning)
+    return _lib.check(int(_lib.load().sarbp_mixed_workspace_size(C.byref(scene.struct()),
+                                                                  C.byref(t))))
+
+
+def focus(scene: DeviceScene, precision: str = "fp64", *, tuning=None,
+          out: torch.Tensor | None = None, diagnostics: bool = False,
+          workspace: torch.Tensor | None = None) -> FocusResult:
+    """Focus a device-resident scene, stream-ordered on torch's current stream.
+
+    ``diagnostics`` also returns per-pixel contributor counts, the (pulse,
+    bin) checksum and, for "mixed", the kernel counters.
+    """
+    if precision not in PRECISIONS:
+        raise ValueError(f"precision must be one of {PRECISIONS}, got {precision!r}")
+    lib = _lib.load()
+    dev = scene.device
+    if out is None:
+        out = torch.empty((scene.npix, 2), dtype=torch.float64, device=dev)
+    res = FocusResult(image=out)
+    nv_ptr = cs_ptr = ctr_ptr = None
+    if diagnostics:
+        res.nvalid = torch.empty(scene.npix, dtype=torch.int32, device=dev)
+        res.checksum = torch.empty(scene.npix, dtype=torch.int64, device=dev)
+        nv_ptr, cs_ptr = res.nvalid.data_ptr(), res.checksum.data_ptr()
+    stream = _stream_ptr(dev)
+    sc = C.byref(scene.struct())
+    if precision == "fp64":
+        _lib.check(lib.sarbp_focus_fp64(sc, out.data_ptr(), nv_ptr, cs_ptr, stream))
+        return res
+    t = resolve_tuning(tuning)
+    need = _lib.check(int(lib.sarbp_mixed_workspace_size(sc, C.byref(t))))
+    if workspace is None or workspace.numel() < need:
+        workspace = torch.empty(need, dtype=torch.uint8, device=dev)
+    if diagnostics:
+        res.counters = torch.zeros(_lib.NUM_COUNTERS, dtype=torch.int64, device=dev)
+        ctr_ptr = res.counters.data_ptr()
+    _lib.check(lib.sarbp_focus_mixed(sc, C.byref(t), out.data_ptr(), nv_ptr, cs_ptr, ctr_ptr,
+                                     workspace.data_ptr(), workspace.numel(), stream))
+    return res
+
+
+def FocalizzatoreBpPx(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
+                      near_range, dra, lambda_val, Sint, *, precision: str = "fp64",
+                      tuning=None, device=None) -> np.ndarray:
+    """Focus one scene; returns complex128 of xxg1's shape (column-major pixels).
+
+    Drop-in for sar_focuser_puntual_noui.py:149 (same positional arguments).
+    """
+    scene = scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
+                            near_range, dra, lambda_val, Sint, device=device)
+    res = focus(scene, precision, tuning=tuning)
+    return res.to_numpy(scene.dim0, scene.dim1)
+
+
+def FocalizzatoreBpCuPy(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
+                        near_range, dra, lambda_val, Sint, **kw) -> np.ndarray:
+    """Same call under gpu_small_dataset.py:113's name."""
+    return FocalizzatoreBpPx(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
+                             near_range, dra, lambda_val, Sint, **kw)
+
+
+def FocalizzatoreBpCuPy_Batched(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
+                                near_range, dra, lambda_val, Sint, batch_size=500000,
+                                **kw) -> np.ndarray:
+    """Same call under gpu_small_dataset.py:229's name.
+
+    ``batch_size`` (pixels per launch in the reference, a memory limit of
+    24 GB cards) is accepted and checked but the scene is focused in one
+    launch: the per-batch host round trips are what this focuser removes.
+    """
+    if int(batch_size) <= 0:
+        raise ValueError("batch_size must be positive")
+    return FocalizzatoreBpPx(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
+                             near_range, dra, lambda_val, Sint, **kw)

@@ -1,0 +1,188 @@
+"""Device-resident focusing scenes.
+
+A scene is the reference's 13 positional focusing arguments
+(sar_focuser_puntual_noui.py:149): DEM x/y/z, mask, index, the trajectory,
+the complex64 raw data, near range, range spacing, wavelength and Sint.  On
+the device every DEM-grid array is flattened in column-major order (as the
+reference flattens them, :183-188) and the raw data are stored pulse-major
+with an even row pitch (range bins of one pulse contiguous, rows 16-byte
+aligned) -- the reference's own column-major RawData byte order, padded when
+Nra is odd.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+
+
+def _as_tensor(a) -> torch.Tensor:
+    if isinstance(a, torch.Tensor):
+        return a
+    return torch.from_numpy(np.asarray(a))
+
+
+def _cast_host(a, np_dtype):
+    """Reference dtype coercion (``astype``) on host arrays; tensors via torch."""
+    if isinstance(a, torch.Tensor):
+        return a.to(getattr(torch, np.dtype(np_dtype).name))
+    a = np.asarray(a)
+    return a if a.dtype == np_dtype else a.astype(np_dtype)
+
+
+def flatten_f(a, np_dtype, device) -> torch.Tensor:
+    """``a.astype(dtype).flatten(order='F')`` as a contiguous device tensor."""
+    a = _cast_host(a, np_dtype)
+    t = _as_tensor(a)
+    if t.dim() > 1:
+        # C-order flatten of the axis-reversed array == F-order flatten
+        t = t.permute(*reversed(range(t.dim())))
+    t = t.to(device, non_blocking=True)
+    return t.contiguous().view(-1)
+
+
+def raw_to_device(raw, device, pitch_multiple: int = 2) -> tuple[torch.Tensor, int, int, int]:
+    """Complex64 (Nra, Naz) raw data -> pulse-major float pairs on the device.
+
+    Returns (tensor of shape (Naz, pitch, 2) float32, nra, naz, pitch) where
+    sample (r, a) is tensor[a, r].
+    """
+    if isinstance(raw, torch.Tensor):
+        t = raw if raw.dtype == torch.complex64 else raw.to(torch.complex64)
+    else:
+        arr = np.asarray(raw)
+        if arr.dtype != np.complex64:
+            arr = arr.astype(np.complex64)
+        t = torch.from_numpy(arr)
+    if t.dim() != 2:
+        raise ValueError("Raw_Data must be a 2D array")
+    nra, naz = int(t.shape[0]), int(t.shape[1])
+    pitch = -(-nra // pitch_multiple) * pitch_multiple
+    tt = t.t()                                    # (naz, nra)
+    if pitch == nra:
+        dev = tt.to(device, non_blocking=True)
+        if not dev.is_contiguous():
+            dev = dev.contiguous()
+        out = torch.view_as_real(dev)
+    else:
+        out = torch.zeros((naz, pitch, 2), dtype=torch.float32, device=device)
+        out[:, :nra, :] = torch.view_as_real(tt.to(device, non_blocking=True))
+    return out, nra, naz, pitch
+
+
+@dataclass
+class DeviceScene:
+    """One focusing scene resident in device memory."""
+
+    dim0: int
+    dim1: int
+    x: torch.Tensor
+    y: torch.Tensor
+    z: torch.Tensor
+    mask: torch.Tensor
+    index: torch.Tensor
+    sint: torch.Tensor
+    tx: torch.Tensor
+    ty: torch.Tensor
+    tz: torch.Tensor
+    raw: torch.Tensor          # (naz, pitch, 2) float32
+    nra: int
+    naz: int
+    pitch: int
+    near_range: float
+    delta_range: float
+    lambda_: float
+    _struct: _lib.Scene | None = field(default=None, repr=False)
+
+    @property
+    def npix(self) -> int:
+        return self.dim0 * self.dim1
+
+    @property
+    def device(self) -> torch.device:
+        return self.raw.device
+
+    def struct(self) -> _lib.Scene:
+        """The C ``sarbp_scene`` view of this scene (device pointers)."""
+        if self._struct is None:
+            s = _lib.Scene()
+            s.dim0, s.dim1 = self.dim0, self.dim1
+            s.dem_x, s.dem_y, s.dem_z = self.x.data_ptr(), self.y.data_ptr(), self.z.data_ptr()
+            s.mask, s.index, s.sint = (self.mask.data_ptr(), self.index.data_ptr(),
+                                       self.sint.data_ptr())
+            s.traj_x, s.traj_y, s.traj_z = (self.tx.data_ptr(), self.ty.data_ptr(),
+                                            self.tz.data_ptr())
+            s.raw = self.raw.data_ptr()
+            s.nra, s.naz, s.raw_pitch = self.nra, self.naz, self.pitch
+            s.near_range, s.delta_range, s.lambda_ = (self.near_range, self.delta_range,
+                                                      self.lambda_)
+            self._struct = s
+        return self._struct
+
+    def nominal_pixel_pulses(self) -> int:
+        """Sum over pixels with mask==1 and Sint != -9999 of ceil(Sint/2)*2+1.
+
+        The implementation-independent unit of work (pixel-pulse back-
+        projections), computed from the inputs.
+        """
+        s = self.sint.to(torch.int64)
+        ok = (self.mask == 1) & (self.sint != -9999)
+        half = torch.where(s >= 0, (s + 1) // 2, -((-s) // 2))
+        jj = half * 2 + 1
+        return int(torch.where(ok & (jj > 0), jj, torch.zeros_like(jj)).sum().item())
+
+    def nbytes(self) -> int:
+        ts = (self.x, self.y, self.z, self.mask, self.index, self.sint, self.tx, self.ty,
+              self.tz, self.raw)
+        return sum(t.numel() * t.element_size() for t in ts)
+
+
+def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
+                    near_range, dra, lambda_val, Sint, device=None) -> DeviceScene:
+    """Upload the reference's 13 focusing arguments (same order) to the device.
+
+    Raises ValueError where the reference does (Raw_Data or xxg1 not 2-D,
+    sar_focuser_puntual_noui.py:163-170) and for arrays whose sizes do not
+    match the DEM grid or a trajectory shorter than Naz (where the reference
+    would fail with an IndexError inside its pixel loop).
+    """
+    raw_shape = tuple(Raw_Data.shape)
+    if len(raw_shape) != 2:
+        raise ValueError("Raw_Data must be a 2D array")
+    if len(tuple(xxg1.shape)) != 2:
+        raise ValueError("xxg1 must be a 2D array")
+    dim0, dim1 = (int(v) for v in xxg1.shape)
+    npix = dim0 * dim1
+    nra, naz = (int(v) for v in raw_shape)
+    for name, a in (("yyg1", yyg1), ("zzg1", zzg1), ("mask", mask), ("index", index),
+                    ("Sint", Sint)):
+        size = int(np.prod(tuple(a.shape)))
+        if size != npix:
+            raise ValueError(f"{name} has {size} elements, the DEM grid has {npix}")
+    for name, w in (("wgsx", wgsx), ("wgsy", wgsy), ("wgsz", wgsz)):
+        if int(np.prod(tuple(w.shape))) < naz:
+            raise ValueError(f"{name} is shorter than Raw_Data's {naz} pulses")
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("sar_backprojection_gb300 needs a CUDA device (no CPU fallback)")
+    device = (torch.device(device) if device is not None
+              else torch.device("cuda", torch.cuda.current_device()))
+    raw_t, nra, naz, pitch = raw_to_device(Raw_Data, device)
+
+    def traj(w):
+        t = _as_tensor(_cast_host(w, np.float64)).reshape(-1)
+        return t.to(device, non_blocking=True).contiguous()
+
+    return DeviceScene(
+        dim0=dim0, dim1=dim1,
+        x=flatten_f(xxg1, np.float64, device), y=flatten_f(yyg1, np.float64, device),
+        z=flatten_f(zzg1, np.float64, device),
+        mask=flatten_f(mask, np.uint8, device), index=flatten_f(index, np.int32, device),
+        sint=flatten_f(Sint, np.int32, device),
+        tx=traj(wgsx), ty=traj(wgsy), tz=traj(wgsz),
+        raw=raw_t, nra=nra, naz=naz, pitch=pitch,
+        near_range=float(near_range), delta_range=float(dra), lambda_=float(lambda_val),
+    )

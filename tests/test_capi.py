@@ -1,0 +1,97 @@
+"""The C-ABI library builds, loads and exports what include/*.h declares.
+
+CPU-only: only calls that fail argument validation before touching CUDA are
+made here.
+"""
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+from sar_backprojection_gb300 import _lib
+from sar_backprojection_gb300 import build as sbuild
+
+INCLUDE = Path(__file__).resolve().parent.parent / "include"
+
+
+def declared_symbols():
+    names = set()
+    for h in INCLUDE.glob("*.h"):
+        text = h.read_text()
+        names.update(re.findall(r"SARBP_API\s+[\w\s\*]+?\b(sarbp_\w+)\s*\(", text))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    assert "sarbp_focus_fp64" in syms and "sarbp_focus_mixed" in syms
+    assert len(syms) >= 6
+
+
+def test_library_exports_every_declared_symbol():
+    lib = C.CDLL(str(sbuild.build_library()))
+    for name in declared_symbols():
+        assert hasattr(lib, name), f"{name} declared in include/ but not exported"
+
+
+def test_python_binding_covers_header():
+    assert set(declared_symbols()) <= set(_lib.SIGNATURES)
+
+
+def test_struct_layout_matches_header():
+    # sarbp_scene: 2 int64 + 10 pointers + 3 int64 + 3 doubles
+    assert C.sizeof(_lib.Scene) == 8 * (2 + 10 + 3 + 3)
+    assert C.sizeof(_lib.Tuning) == 4 * 8
+
+
+def test_version_and_defaults():
+    lib = _lib.load()
+    assert lib.sarbp_version() >= 100
+    t = _lib.default_tuning()
+    assert t.chunk in (32, 64) and t.tile0 > 0 and t.tile1 > 0
+
+
+def test_null_scene_is_rejected_with_message():
+    lib = _lib.load()
+    rc = lib.sarbp_focus_fp64(None, None, None, None, None)
+    assert rc == _lib.SARBP_EINVAL
+    assert "NULL" in _lib.last_error()
+    with pytest.raises(_lib.SarbpError):
+        _lib.check(rc)
+
+
+def test_bad_shapes_are_rejected():
+    lib = _lib.load()
+    s = _lib.Scene()
+    s.dim0, s.dim1 = 4, 4
+    for f in ("dem_x", "dem_y", "dem_z", "mask", "index", "sint", "traj_x", "traj_y",
+              "traj_z", "raw"):
+        setattr(s, f, 0x1000)                  # never dereferenced: validation fails first
+    s.nra, s.naz, s.raw_pitch = 8, 16, 4      # pitch < nra
+    s.delta_range, s.lambda_ = 0.5, 0.031
+    out = C.c_void_p(0x2000)
+    assert lib.sarbp_focus_fp64(C.byref(s), out, None, None, None) == _lib.SARBP_EINVAL
+    assert "raw_pitch" in _lib.last_error()
+    s.raw_pitch = 8
+    s.delta_range = 0.0
+    assert lib.sarbp_focus_fp64(C.byref(s), out, None, None, None) == _lib.SARBP_EINVAL
+    s.delta_range = 0.5
+    s.dim0 = 0
+    assert lib.sarbp_focus_fp64(C.byref(s), out, None, None, None) == _lib.SARBP_EINVAL
+
+
+def test_workspace_size_is_host_only():
+    lib = _lib.load()
+    s = _lib.Scene()
+    s.dim0, s.dim1 = 4000, 250
+    for f in ("dem_x", "dem_y", "dem_z", "mask", "index", "sint", "traj_x", "traj_y",
+              "traj_z", "raw"):
+        setattr(s, f, 0x1000)
+    s.nra, s.naz, s.raw_pitch = 4762, 40001, 4762
+    s.delta_range, s.lambda_, s.near_range = 0.5, 0.031, 3500.0
+    t = _lib.default_tuning()
+    n = lib.sarbp_mixed_workspace_size(C.byref(s), C.byref(t))
+    assert n >= 16 * 40001
+    t.chunk = 48
+    assert lib.sarbp_mixed_workspace_size(C.byref(s), C.byref(t)) == _lib.SARBP_EINVAL

@@ -1,0 +1,62 @@
+"""Host-side behaviour of the drop-in focusing call (no GPU needed)."""
+import numpy as np
+import pytest
+import torch
+
+from sar_backprojection_gb300 import FocalizzatoreBpPx, FocalizzatoreBpCuPy_Batched, synth
+from sar_backprojection_gb300.scene import flatten_f
+
+
+def _args():
+    return list(synth.focus_args(synth.generate(synth.config_small())))
+
+
+def test_raw_data_must_be_2d():
+    a = _args()
+    a[8] = a[8].reshape(-1)
+    with pytest.raises(ValueError, match="Raw_Data must be a 2D array"):
+        FocalizzatoreBpPx(*a)
+
+
+def test_dem_must_be_2d():
+    a = _args()
+    a[0] = a[0].reshape(-1)
+    with pytest.raises(ValueError, match="xxg1 must be a 2D array"):
+        FocalizzatoreBpPx(*a)
+
+
+def test_size_mismatch_and_short_trajectory():
+    a = _args()
+    a[3] = a[3][:-1]
+    with pytest.raises(ValueError, match="mask"):
+        FocalizzatoreBpPx(*a)
+    a = _args()
+    a[5] = a[5][:100]
+    with pytest.raises(ValueError, match="wgsx"):
+        FocalizzatoreBpPx(*a)
+
+
+def test_batched_rejects_bad_batch_size():
+    with pytest.raises(ValueError):
+        FocalizzatoreBpCuPy_Batched(*_args(), batch_size=0)
+
+
+@pytest.mark.skipif(torch.cuda.is_available(), reason="checks the no-GPU error")
+def test_no_cpu_fallback():
+    with pytest.raises(RuntimeError, match="CUDA"):
+        FocalizzatoreBpPx(*_args())
+
+
+def test_flatten_matches_numpy_fortran_order():
+    a = np.arange(24, dtype=np.int64).reshape(4, 6)
+    for arr in (a, np.asfortranarray(a)):
+        t = flatten_f(arr, np.int32, "cpu")
+        assert t.dtype == torch.int32
+        assert np.array_equal(t.numpy(), arr.astype(np.int32).flatten(order="F"))
+    # reference dtype coercion: float index truncates, uint8 wraps
+    f = np.array([[1.7, -2.2], [3.9, 4.0]])
+    assert np.array_equal(flatten_f(f, np.int32, "cpu").numpy(),
+                          f.astype(np.int32).flatten(order="F"))
+    m = np.array([[257, 1], [2, -255]])
+    assert np.array_equal(flatten_f(m, np.uint8, "cpu").numpy(),
+                          m.astype(np.uint8).flatten(order="F"))
