@@ -47,7 +47,7 @@ DATA = "synthetic (seeded: 200 point targets + slope-weighted clutter, motion +-
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--fp64-steps", type=int, default=2)
@@ -57,7 +57,20 @@ def parse():
     ap.add_argument("--tuning", type=str, default="",
                     help="chunk,tile0,tile1[,staged] of the mixed kernel")
     ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--workload", choices=["full", "profile"], default="full",
+                    help="profile: the same geometry at 1000x250 pixels / 10001 pulses "
+                         "(381 MB of raw data), a small case for ncu captures")
     return ap.parse_args()
+
+
+def workload_spec(args, rank: int):
+    from sar_backprojection_gb300 import synth
+    if args.workload == "profile":
+        return (synth.scaled_full(args.seed + rank, 1000, 250, 10001, 1200, 1800,
+                                  name="profile_1000x250_10001"),
+                "profile_1000x250_10001: config_full geometry at DEM 1000x250, 10001 pulses, "
+                "Nra 4762 (381 MB complex64)")
+    return synth.config_full(args.seed + rank), WORKLOAD
 
 
 # ----------------------------------------------------------------------------
@@ -116,7 +129,7 @@ class ClockSampler:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+                 "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
 
@@ -225,7 +238,7 @@ def run_reference(args, dist: Dist):
     from oracle import oracle
     from sar_backprojection_gb300 import synth
 
-    spec = synth.config_full(args.seed)
+    spec, workload_name = workload_spec(args, 0)
     dev = "cuda" if torch.cuda.is_available() else "cpu"
     scene = synth.generate(spec, raw_device=dev)        # input synthesis only
     host = host_scene_of(scene)
@@ -246,7 +259,7 @@ def run_reference(args, dist: Dist):
         "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": DATA,
-        "config": {"workload": WORKLOAD, "precision": "fp64 (reference semantics)",
+        "config": {"workload": workload_name, "precision": "fp64 (reference semantics)",
                    "implementation": "oracle C restatement of process_point/"
                                      "FocalizzatoreBpPx, OpenMP over pixels",
                    "l2": "host run (no GPU)"},
@@ -279,7 +292,7 @@ def run_ours(args, dist: Dist):
         for k, v in zip(("chunk", "tile0", "tile1", "staged"), vals):
             setattr(tuning, k, v)
 
-    spec = synth.config_full(args.seed + dist.rank)
+    spec, workload_name = workload_spec(args, dist.rank)
     scene = synth.generate(spec, raw_device=str(dev))
     ds = scene_to_device(*synth.focus_args(scene), device=dev)
     work = ds.nominal_pixel_pulses()
@@ -328,23 +341,29 @@ def run_ours(args, dist: Dist):
 
     # the plain FP64 kernel on the same scene (comparator), and quality
     mixed_img = out.clone()
-    f64 = focus(ds, "fp64")
-    torch.cuda.synchronize(dev)
-    f_ms = []
-    for _ in range(args.fp64_steps):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        focus(ds, "fp64", out=f64.image)
-        b.record(stream)
+    fp64_ms = None
+    q = None
+    if args.fp64_steps > 0:
+        f64 = focus(ds, "fp64")
         torch.cuda.synchronize(dev)
-        f_ms.append(a.elapsed_time(b))
-    fp64_ms = statistics.mean(f_ms)
-    q = quality.compare(mixed_img.cpu().numpy(), f64.image.cpu().numpy())
+        f_ms = []
+        for _ in range(args.fp64_steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            focus(ds, "fp64", out=f64.image)
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            f_ms.append(a.elapsed_time(b))
+        fp64_ms = statistics.mean(f_ms)
+        q = quality.compare(mixed_img.cpu().numpy(), f64.image.cpu().numpy())
+        del f64
     dm = focus(ds, "mixed", tuning=tuning, diagnostics=True)
-    df = focus(ds, "fp64", diagnostics=True)
+    df = focus(ds, "fp64", diagnostics=True) if args.fp64_steps > 0 else None
     torch.cuda.synchronize(dev)
-    bins_exact = bool(torch.equal(dm.nvalid, df.nvalid) and torch.equal(dm.checksum, df.checksum))
+    bins_exact = (bool(torch.equal(dm.nvalid, df.nvalid) and torch.equal(dm.checksum, df.checksum))
+                  if df is not None else None)
     counters = dm.counters.cpu().tolist()
+    del dm, df
 
     # roofline of the main kernel
     rates = (C.c_double * 4)()
@@ -353,7 +372,7 @@ def run_ours(args, dist: Dist):
     peak = roofline.peak_pixel_pulses(ffma, sfu) / 1e9
     achieved = work / (kernel_ms * 1e-3) / 1e9
     peak64 = roofline.peak_pixel_pulses_fp64(dfma) / 1e9
-    achieved64 = work / (fp64_ms * 1e-3) / 1e9
+    achieved64 = work / (fp64_ms * 1e-3) / 1e9 if fp64_ms else None
     idx = ds.index.to(torch.int64)
     s = ds.sint.to(torch.int64)
     active = (ds.mask == 1) & (ds.sint != -9999)
@@ -363,7 +382,7 @@ def run_ours(args, dist: Dist):
     alg_bytes = roofline.algorithmic_bytes(ds.npix, ds.naz, ds.nra, hi - lo + 1)
     hbm_peak = measured_peaks().get("hbm_gbs")
     hbm_achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
-    traffic = profile_traffic("focus_mixed_main:full_4000x250_40001")
+    traffic = profile_traffic(f"focus_mixed_main:{spec.name}")
 
     # end to end through the drop-in call, pinned host inputs
     e2e = None
@@ -425,18 +444,19 @@ def run_ours(args, dist: Dist):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 per pulse + f64 per chunk reference (mixed)", "data": DATA,
-            "config": {"workload": WORKLOAD, "precision": "mixed",
+            "config": {"workload": workload_name, "precision": "mixed",
                        "nominal_pixel_pulses_per_scene": work,
                        "tuning": tuning.as_dict(),
                        "l2": "inputs larger than L2 (1.52 GB raw data re-read every step)",
                        "scenes": f"one per GPU (seed {args.seed}+rank)"},
-            "fp64": {"value": dist.world * work / (fp64_ms * 1e-3) / 1e9, "unit": UNIT,
-                     "ms_per_step": fp64_ms, "steps": args.fp64_steps},
-            "speedup_mixed_vs_fp64": fp64_ms / ms_per_step,
-            "quality": {"vs": "FP64 kernel (bit-exact bins with the oracle)",
-                        "coherence": q["coherence"], "rms_phase_mrad": q["rms_phase_mrad"],
-                        "rel_l2": q["rel_l2"], "bins_bit_exact": bins_exact,
-                        "ambiguous_bins_rederived": counters[_lib.CTR_AMBIGUOUS]},
+            "fp64": ({"value": dist.world * work / (fp64_ms * 1e-3) / 1e9, "unit": UNIT,
+                      "ms_per_step": fp64_ms, "steps": args.fp64_steps} if fp64_ms else None),
+            "speedup_mixed_vs_fp64": fp64_ms / ms_per_step if fp64_ms else None,
+            "quality": ({"vs": "FP64 kernel (bit-exact bins with the oracle)",
+                         "coherence": q["coherence"], "rms_phase_mrad": q["rms_phase_mrad"],
+                         "rel_l2": q["rel_l2"], "bins_bit_exact": bins_exact,
+                         "ambiguous_bins_rederived": counters[_lib.CTR_AMBIGUOUS]}
+                        if q else {"ambiguous_bins_rederived": counters[_lib.CTR_AMBIGUOUS]}),
             "latency": lat,
             "roofline": {"bound": "fp32_sfu_issue", "achieved": achieved, "peak": peak,
                          "unit": UNIT, "frac": achieved / peak, "traffic": traffic,
@@ -451,7 +471,7 @@ def run_ours(args, dist: Dist):
                              "traffic": traffic, "algorithmic_bytes": alg_bytes,
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
             "roofline_fp64": {"bound": "fp64_issue", "achieved": achieved64, "peak": peak64,
-                              "unit": UNIT, "frac": achieved64 / peak64,
+                              "unit": UNIT, "frac": achieved64 / peak64 if achieved64 else None,
                               "peak_source": f"probe FP64 FMA {dfma / 1e12:.2f} Tlane/s "
                                              f"/{roofline.N_FP64}"},
             "cpu_baseline": cpu,

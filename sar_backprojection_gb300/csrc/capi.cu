@@ -80,6 +80,19 @@ bool build_params(const sarbp_scene *s, SceneParams *p)
     p->beta = four * pi * alfa / (c * c);
     p->k4pl = -four * pi / s->lambda;
     p->inv_dra = 1.0 / s->delta_range;
+    auto split = [](double d, float &h, float &l) {
+        h = (float)d;
+        l = (float)(d - (double)h);
+    };
+    const double two_pi = 6.283185307179586477;
+    split(s->near_range, p->near_hi, p->near_lo);
+    split(p->inv_dra, p->idra_hi, p->idra_lo);
+    split(p->k4pl / two_pi, p->k1_hi, p->k1_lo);
+    split(p->beta / two_pi, p->k2_hi, p->k2_lo);
+    p->k4pl_f = (float)p->k4pl;
+    p->beta_f = (float)p->beta;
+    p->beta2_f = (float)(2.0 * p->beta);
+    p->inv_dra_f = (float)p->inv_dra;
     return true;
 }
 

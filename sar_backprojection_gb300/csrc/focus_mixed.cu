@@ -1,11 +1,12 @@
 // focus_mixed.cu -- mixed-precision pixel-tiled back-projection.
 //
 // Work decomposition: one CTA per pixel tile (tile0 x tile1 pixels of the
-// column-major DEM grid, one thread per pixel); the union of the tile's
-// apertures is walked in pulse chunks aligned to multiples of `chunk`.
-// Precision plan: mixed_common.cuh.  This file holds the chunk-table prep
-// kernel, the L1/L2-gather main kernel and the launch logic; the TMA-staged
-// main kernel lives in focus_staged.cu.
+// column-major DEM grid, one thread per pixel, each warp an 8 x 4 block of
+// neighbouring pixels so that its lanes share apertures and range bins); the
+// union of the tile's apertures is walked in pulse chunks aligned to
+// multiples of `chunk`.  Precision plan: mixed_common.cuh.  This file holds
+// the chunk-table prep kernel, the L1/L2-gather main kernel and the launch
+// logic.
 #include <climits>
 #include <cstdio>
 
@@ -19,24 +20,27 @@ MixedLayout mixed_layout(int64_t naz, int chunk)
 {
     MixedLayout L{};
     size_t off = align256(sizeof(StatusBlock));
-    L.ptab = off;
-    off = align256(off + sizeof(float4) * (size_t)naz);
-    L.ctab = off;
     const int64_t nchunks = (naz + chunk - 1) / chunk;
-    off = align256(off + sizeof(float4) * (size_t)nchunks);
+    L.ptab = off;      // padded to whole chunks: the staged kernel copies whole chunks
+    off = align256(off + sizeof(float4) * (size_t)(nchunks * chunk));
+    L.pff = off;
+    off = align256(off + sizeof(PulseFF) * (size_t)naz);
+    L.ctab = off;
+    off = align256(off + sizeof(ChunkRef) * (size_t)nchunks);
     L.total = off;
     return L;
 }
 
-__device__ __forceinline__ int64_t chunk_ref(int64_t c, int chunk, int64_t naz)
+__host__ __device__ __forceinline__ int64_t chunk_ref(int64_t c, int chunk, int64_t naz)
 {
     const int64_t k0 = c * chunk + chunk / 2;
     return k0 < naz - 1 ? k0 : naz - 1;
 }
 
-// Per-pulse chunk table and per-chunk bounds; one warp per chunk.
+// Per-pulse tables and per-chunk references; one warp per chunk.
 __global__ void chunk_table_kernel(const SceneParams P, int chunk, float4 *__restrict__ ptab,
-                                   float4 *__restrict__ ctab, int64_t nchunks)
+                                   PulseFF *__restrict__ pff, ChunkRef *__restrict__ ctab,
+                                   int64_t nchunks)
 {
     const int64_t c = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     const int lane = threadIdx.x & 31;
@@ -47,38 +51,79 @@ __global__ void chunk_table_kernel(const SceneParams P, int chunk, float4 *__res
     for (int j = lane; j < chunk; j += 32) {
         const int64_t k = c * chunk + j;
         if (k >= P.naz) break;
-        const double ex = P.tx[k] - x0, ey = P.ty[k] - y0, ez = P.tz[k] - z0;
+        const double tx = P.tx[k], ty = P.ty[k], tz = P.tz[k];
+        const double ex = tx - x0, ey = ty - y0, ez = tz - z0;
         const double e2 = ex * ex + ey * ey + ez * ez;
         const float4 e = make_float4((float)ex, (float)ey, (float)ez, (float)e2);
         ptab[k] = e;
+        PulseFF f;
+        split_ff(tx, f.hi.x, f.lo.x);
+        split_ff(ty, f.hi.y, f.lo.y);
+        split_ff(tz, f.hi.z, f.lo.z);
+        f.hi.w = f.lo.w = 0.f;
+        pff[k] = f;
         // Bounds rounded up by one part in 2^20 so they hold for the FP32 values.
         mx = fmaxf(mx, fabsf(e.x) * 1.000001f);
         my = fmaxf(my, fabsf(e.y) * 1.000001f);
         mz = fmaxf(mz, fabsf(e.z) * 1.000001f);
         m2 = fmaxf(m2, e.w * 1.000001f);
     }
+    // Largest distance of the chunk's pulses from the chord between its first
+    // and last pulse (bounds the staged kernel's range windows).
+    const int64_t ka = c * chunk, kb = min(c * chunk + chunk - 1, P.naz - 1);
+    const double ax = P.tx[ka], ay = P.ty[ka], az = P.tz[ka];
+    const double sx = P.tx[kb] - ax, sy = P.ty[kb] - ay, sz = P.tz[kb] - az;
+    const double ss = sx * sx + sy * sy + sz * sz;
+    double dev = 0.0;
+    for (int64_t k = ka + lane; k <= kb; k += 32) {
+        const double qx = P.tx[k] - ax, qy = P.ty[k] - ay, qz = P.tz[k] - az;
+        const double u = ss > 0.0 ? (qx * sx + qy * sy + qz * sz) / ss : 0.0;
+        const double rx = qx - u * sx, ry = qy - u * sy, rz = qz - u * sz;
+        dev = fmax(dev, sqrt(rx * rx + ry * ry + rz * rz));
+    }
     for (int o = 16; o > 0; o >>= 1) {
         mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         my = fmaxf(my, __shfl_xor_sync(0xffffffffu, my, o));
         mz = fmaxf(mz, __shfl_xor_sync(0xffffffffu, mz, o));
         m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+        dev = fmax(dev, __shfl_xor_sync(0xffffffffu, dev, o));
     }
-    if (lane == 0) ctab[c] = make_float4(mx, my, mz, m2);
+    if (lane == 0) {
+        ChunkRef r;
+        r.emax = make_float4(mx, my, mz, m2);
+        split_ff(x0, r.thi.x, r.tlo.x);
+        split_ff(y0, r.thi.y, r.tlo.y);
+        split_ff(z0, r.thi.z, r.tlo.z);
+        r.thi.w = (float)dev + 1.0e-3f;     // chord deviation + margin (m)
+        r.tlo.w = 0.f;
+        ctab[c] = r;
+    }
+}
+
+// Pixel of thread t in a tile: warps are 8 (dim0) x 4 (dim1) pixel blocks.
+template <int T0, int T1>
+__device__ __forceinline__ void tile_pixel(int t, int64_t tile0, int64_t tile1, int64_t &i0,
+                                           int64_t &i1)
+{
+    static_assert(T0 % 8 == 0 && T1 % 4 == 0, "tile must be a multiple of the 8x4 warp block");
+    const int w = t >> 5, lane = t & 31;
+    i0 = tile0 * T0 + (w % (T0 / 8)) * 8 + (lane & 7);
+    i1 = tile1 * T1 + (w / (T0 / 8)) * 4 + (lane >> 3);
 }
 
 // Main kernel, raw samples gathered through L1/L2.
 template <int CHUNK, int T0, int T1, bool kChecksum>
 __global__ void __launch_bounds__(T0 *T1)
 focus_mixed_gather_kernel(const SceneParams P, const float4 *__restrict__ ptab,
-                          const float4 *__restrict__ ctab, int64_t ntile0,
-                          double2 *__restrict__ out, int32_t *__restrict__ nvalid,
-                          uint64_t *__restrict__ checksum, unsigned long long *__restrict__ counters)
+                          const PulseFF *__restrict__ pff, const ChunkRef *__restrict__ ctab,
+                          int64_t ntile0, double2 *__restrict__ out, int32_t *__restrict__ nvalid,
+                          uint64_t *__restrict__ checksum,
+                          unsigned long long *__restrict__ counters)
 {
     __shared__ long long s_lo, s_hi;
     const int t = threadIdx.x;
-    const int64_t tile = blockIdx.x;
-    const int64_t i0 = (tile % ntile0) * T0 + (t % T0);
-    const int64_t i1 = (tile / ntile0) * T1 + (t / T0);
+    int64_t i0, i1;
+    tile_pixel<T0, T1>(t, blockIdx.x % ntile0, blockIdx.x / ntile0, i0, i1);
     const bool inside = i0 < P.dim0 && i1 < P.dim1;
     const int64_t ii = inside ? i0 + P.dim0 * i1 : 0;
     int64_t lo = 0, hi = -1;
@@ -97,67 +142,66 @@ focus_mixed_gather_kernel(const SceneParams P, const float4 *__restrict__ ptab,
     __syncthreads();
     const int64_t tlo = s_lo, thi = s_hi;
 
-    double px = 0.0, py = 0.0, pz = 0.0;
-    if (active) {
-        px = P.x[ii];
-        py = P.y[ii];
-        pz = P.z[ii];
-    }
+    PixelFF pf{};
+    if (active) pf = pixel_ff(P.x[ii], P.y[ii], P.z[ii]);
     float acc_re = 0.f, acc_im = 0.f, cmp_re = 0.f, cmp_im = 0.f;
     int n = 0;
     uint64_t cs = 0;
     unsigned ambiguous = 0, chunks = 0;
-    const float inv_dra_f = (float)P.inv_dra;
-    const float beta_f = (float)P.beta;
     const unsigned nra_m1 = (unsigned)(P.nra - 1);
+    const int pitch = (int)P.pitch;
 
     if (thi >= 0) {
         for (int64_t c = tlo / CHUNK; c <= thi / CHUNK; ++c) {
             const int64_t K = c * CHUNK;
-            const int64_t kmin = lo > K ? lo : K;
-            const int64_t kmax = hi < K + CHUNK - 1 ? hi : K + CHUNK - 1;
-            if (!active || kmin > kmax) continue;
+            const int jmin = (int)(lo > K ? lo - K : 0);
+            const int jmax = (int)(hi < K + CHUNK - 1 ? hi - K : CHUNK - 1);
+            if (!active || jmin > jmax) continue;
             ++chunks;
+            ChunkRef ref;
+            ref.emax = __ldg(&ctab[c].emax);
+            ref.thi = __ldg(&ctab[c].thi);
+            ref.tlo = __ldg(&ctab[c].tlo);
             ChunkSetup S;
-            chunk_setup(P, px, py, pz, chunk_ref(c, CHUNK, P.naz), __ldg(ctab + c), S);
+            chunk_setup(P, pf, ref, S);
             if (S.exact) {
+                const double px = P.x[ii], py = P.y[ii], pz = P.z[ii];
                 double sre = 0.0, sim = 0.0;
-                for (int64_t a = kmin; a <= kmax; ++a) {
+                for (int j = jmin; j <= jmax; ++j) {
                     int64_t bin;
                     double tre, tim;
-                    if (exact_term(P, px, py, pz, a, &bin, &tre, &tim)) {
+                    if (exact_term(P, px, py, pz, K + j, &bin, &tre, &tim)) {
                         sre += tre;
                         sim += tim;
                         ++n;
-                        if (kChecksum) cs += mix64(a, bin);
+                        if (kChecksum) cs += mix64(K + j, bin);
                     }
                 }
                 kahan_add(acc_re, cmp_re, (float)sre);
                 kahan_add(acc_im, cmp_im, (float)sim);
                 continue;
             }
+            const float4 *ep = ptab + K;
+            const float2 *rowc = P.raw + K * P.pitch;
+            const float tie = 0.5f - S.eps;
             float sre = 0.f, sim = 0.f;
-            const float2 *row = P.raw + kmin * P.pitch;
-            for (int64_t k = kmin; k <= kmax; ++k, row += P.pitch) {
-                const float4 e = __ldg(ptab + k);
+#pragma unroll 4
+            for (int j = jmin; j <= jmax; ++j) {
+                const float4 e = __ldg(ep + j);
                 const float D = fmaf(S.mx, e.x, fmaf(S.my, e.y, fmaf(S.mz, e.z, e.w)));
                 const float dR = D * fmaf(fmaf(S.c3, D, S.c2), D, S.c1);
-                const float g = fmaf(dR, inv_dra_f, S.g0);
-                const float rnd = __fadd_rn(g, 12582912.0f);
-                int bin = S.n0 + (__float_as_int(rnd) - 0x4B400000);
-                const float fr = __fsub_rn(g, __fsub_rn(rnd, 12582912.0f));
-                if (fabsf(fr) > kAmbiguity) {
-                    double r2, r;
-                    const int64_t eb = exact_bin(px, py, pz, __ldg(P.tx + k), __ldg(P.ty + k),
-                                                 __ldg(P.tz + k), P.near_range, P.dra, P.nra,
-                                                 &r2, &r);
-                    bin = (int)eb;
+                const float g = fmaf(dR, P.inv_dra_f, S.g0);
+                int ib;
+                const float gr = round_shift(g, ib);
+                int bin = S.n0 + ib;
+                if (fabsf(__fsub_rn(g, gr)) > tie) {
+                    bin = resolve_bin(P, pf, ii, pff, K + j);
                     ++ambiguous;
                 }
                 const bool ok = (unsigned)bin < nra_m1;
                 float2 v = make_float2(0.f, 0.f);
-                if (ok) v = __ldg(row + bin);
-                const float ph = dR * fmaf(beta_f, dR, S.a);
+                if (ok) v = __ldg(rowc + (j * pitch + bin));
+                const float ph = dR * fmaf(P.beta_f, dR, S.a);
                 float sn, cn;
                 __sincosf(ph, &sn, &cn);
                 const float tre = fmaf(v.x, cn, v.y * sn);
@@ -166,7 +210,7 @@ focus_mixed_gather_kernel(const SceneParams P, const float4 *__restrict__ ptab,
                 sre = fmaf(w, tre, sre);
                 sim = fmaf(w, tim, sim);
                 n += ok ? 1 : 0;
-                if (kChecksum && ok) cs += mix64(k, bin);
+                if (kChecksum && ok) cs += mix64(K + j, bin);
             }
             // chunk sum * exp(-j*phi0)
             const float rre = fmaf(sre, S.w0re, -(sim * S.w0im));
@@ -211,16 +255,21 @@ static int launch_gather(const SceneParams &P, const MixedLayout &L, char *ws, d
         return SARBP_ERANGE;
     }
     auto *ptab = reinterpret_cast<const float4 *>(ws + L.ptab);
-    auto *ctab = reinterpret_cast<const float4 *>(ws + L.ctab);
+    auto *pff = reinterpret_cast<const PulseFF *>(ws + L.pff);
+    auto *ctab = reinterpret_cast<const ChunkRef *>(ws + L.ctab);
     auto *ctr = reinterpret_cast<unsigned long long *>(counters);
     if (checksum)
         focus_mixed_gather_kernel<CHUNK, T0, T1, true><<<(unsigned)tiles, T0 * T1, 0, stream>>>(
-            P, ptab, ctab, nt0, reinterpret_cast<double2 *>(out), nvalid, checksum, ctr);
+            P, ptab, pff, ctab, nt0, reinterpret_cast<double2 *>(out), nvalid, checksum, ctr);
     else
         focus_mixed_gather_kernel<CHUNK, T0, T1, false><<<(unsigned)tiles, T0 * T1, 0, stream>>>(
-            P, ptab, ctab, nt0, reinterpret_cast<double2 *>(out), nvalid, nullptr, ctr);
+            P, ptab, pff, ctab, nt0, reinterpret_cast<double2 *>(out), nvalid, nullptr, ctr);
     return cuda_status(cudaGetLastError(), "focus_mixed_gather launch");
 }
+
+int launch_staged(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L, char *ws,
+                  double *out, int32_t *nvalid, uint64_t *checksum, uint64_t *counters,
+                  cudaStream_t stream);
 
 int launch_chunk_table(const SceneParams &P, int chunk, char *ws, const MixedLayout &L,
                        cudaStream_t stream)
@@ -229,8 +278,8 @@ int launch_chunk_table(const SceneParams &P, int chunk, char *ws, const MixedLay
     const int warps = 8;
     const int64_t blocks = (nchunks + warps - 1) / warps;
     chunk_table_kernel<<<(unsigned)blocks, warps * 32, 0, stream>>>(
-        P, chunk, reinterpret_cast<float4 *>(ws + L.ptab), reinterpret_cast<float4 *>(ws + L.ctab),
-        nchunks);
+        P, chunk, reinterpret_cast<float4 *>(ws + L.ptab), reinterpret_cast<PulseFF *>(ws + L.pff),
+        reinterpret_cast<ChunkRef *>(ws + L.ctab), nchunks);
     return cuda_status(cudaGetLastError(), "chunk_table launch");
 }
 
@@ -260,7 +309,14 @@ int launch_mixed_main(const SceneParams &P, const sarbp_tuning &T, void *workspa
     const MixedLayout L = mixed_layout(P.naz, T.chunk);
     int rc = check_workspace(L, workspace, ws_bytes);
     if (rc) return rc;
+    if (P.pitch * (int64_t)T.chunk + P.nra >= (1LL << 31)) {
+        set_error("sarbp mixed path: raw_pitch %lld too large for %d-pulse chunks",
+                  (long long)P.pitch, T.chunk);
+        return SARBP_ERANGE;
+    }
     char *ws = static_cast<char *>(workspace);
+    if (T.staged)
+        return launch_staged(P, T, L, ws, out, nvalid, checksum, counters, stream);
     const int key = T.chunk * 1000000 + T.tile0 * 1000 + T.tile1;
     switch (key) {
         case 32 * 1000000 + 32 * 1000 + 8:

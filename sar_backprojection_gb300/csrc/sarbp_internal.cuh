@@ -28,6 +28,12 @@ struct SceneParams {
     double beta;             // 4*pi*alfa/(c*c)                    (:29)
     double k4pl;             // (-4*pi)/lambda                     (:105)
     double inv_dra;          // 1/dra (reference-range estimate only)
+    // float-float / FP32 forms for the mixed path (hi + lo == value to ~2^-48)
+    float near_hi, near_lo;  // near range
+    float idra_hi, idra_lo;  // 1/dra
+    float k1_hi, k1_lo;      // k4pl/(2*pi), turns per metre
+    float k2_hi, k2_lo;      // beta/(2*pi), turns per square metre
+    float k4pl_f, beta_f, beta2_f, inv_dra_f;
 };
 
 // Aperture of one pixel, clamped to the kept pulses 0 < a < naz-1
@@ -104,7 +110,8 @@ int cuda_status(cudaError_t e, const char *what);
 struct MixedLayout {
     size_t status;   // StatusBlock
     size_t ptab;     // float4[naz]: e = t(k) - t(k0), |e|^2
-    size_t ctab;     // float4[nchunks]: max |e_x|, |e_y|, |e_z|, |e|^2
+    size_t pff;      // PulseFF[naz]: float-float pulse positions
+    size_t ctab;     // ChunkRef[nchunks]: bounds of e and t(k0)
     size_t total;
 };
 MixedLayout mixed_layout(int64_t naz, int chunk);

@@ -25,8 +25,12 @@ MIXED_COHERENCE = 0.9999
 MIXED_RMS_MRAD = 1.0
 MIXED_REL_L2 = 1e-3
 
-TUNINGS = [dict(chunk=c, tile0=t0, tile1=t1) for c in (32, 64)
-           for (t0, t1) in ((32, 8), (64, 4), (16, 16))]
+TUNINGS = ([dict(chunk=c, tile0=t0, tile1=t1, staged=0) for c in (32, 64)
+            for (t0, t1) in ((32, 8), (64, 4), (16, 16))]
+           + [dict(chunk=32, tile0=t0, tile1=t1, staged=1)
+              for (t0, t1) in ((32, 8), (64, 4), (16, 16))])
+TUNING_IDS = [f"c{t['chunk']}_{t['tile0']}x{t['tile1']}_{'tma' if t['staged'] else 'l1'}"
+              for t in TUNINGS]
 
 
 def run(scene, precision, tuning=None):
@@ -93,7 +97,7 @@ def test_mixed_kernel_golden(name):
     assert (img[onv == 0] == 0).all()
 
 
-@pytest.mark.parametrize("tuning", TUNINGS, ids=lambda t: f"c{t['chunk']}_{t['tile0']}x{t['tile1']}")
+@pytest.mark.parametrize("tuning", TUNINGS, ids=TUNING_IDS)
 def test_mixed_kernel_small_workload_tunings(small, tuning):
     scene, ref = small
     img, nv, cs, ctr = run(scene, "mixed", tuning)
@@ -123,18 +127,33 @@ def full_scene():
     return scene
 
 
-def test_full_workload_fp64_and_mixed(full_scene):
-    """4000 x 250 pixels, 40001 pulses: both kernels against the full oracle."""
-    scene = full_scene
-    host = dict(scene)
-    host["RawData"] = scene["RawData"].cpu()          # (nra, naz) view, pulse-major
-    oimg, onv, ocs = oracle.focus_scene(host)
-    img, nv, cs, _ = run(scene, "fp64")
+@pytest.fixture(scope="module")
+def full_oracle(full_scene):
+    host = dict(full_scene)
+    host["RawData"] = full_scene["RawData"].cpu()     # (nra, naz) view, pulse-major
+    return oracle.focus_scene(host)
+
+
+def test_full_workload_fp64(full_scene, full_oracle):
+    """4000 x 250 pixels, 40001 pulses: FP64 kernel against the full oracle."""
+    oimg, onv, ocs = full_oracle
+    img, nv, cs, _ = run(full_scene, "fp64")
     assert np.array_equal(nv, onv) and np.array_equal(cs, ocs)
     assert_fp64_close(img, oimg)
-    mimg, mnv, mcs, ctr = run(scene, "mixed")
+
+
+@pytest.mark.parametrize("tuning", [dict(chunk=64, tile0=32, tile1=8, staged=0),
+                                    dict(chunk=32, tile0=32, tile1=8, staged=0),
+                                    dict(chunk=32, tile0=32, tile1=8, staged=1),
+                                    dict(chunk=32, tile0=64, tile1=4, staged=1)],
+                         ids=["c64_l1", "c32_l1", "c32_32x8_tma", "c32_64x4_tma"])
+def test_full_workload_mixed(full_scene, full_oracle, tuning):
+    """Mixed kernel variants against the full oracle image."""
+    oimg, onv, ocs = full_oracle
+    mimg, mnv, mcs, ctr = run(full_scene, "mixed", tuning)
     assert np.array_equal(mnv, onv) and np.array_equal(mcs, ocs)
     q = assert_mixed_quality(mimg, oimg)
-    print("full workload mixed vs oracle:", {k: q[k] for k in ("rel_l2", "coherence",
-                                                                 "rms_phase_mrad")},
+    assert ctr[3] == 0                                 # no bounded wait gave up
+    print("full workload mixed", tuning, {k: q[k] for k in ("rel_l2", "coherence",
+                                                             "rms_phase_mrad")},
           "counters:", ctr[:4])
