@@ -71,8 +71,11 @@ typedef struct sarbp_scene {
 } sarbp_scene;
 
 /*
- * Tuning of the mixed-precision kernel.  Zero-initialised fields take the
- * library default; sarbp_default_tuning() fills the defaults explicitly.
+ * Tuning of the mixed-precision kernel.  An all-zero struct (or NULL) selects
+ * the library default (TMA-staged, 32-pulse chunks, 16 x 16 pixel tiles);
+ * sarbp_default_tuning() fills the defaults explicitly.  Supported: staged=0
+ * with chunk 32/64 and tiles 32x8, 64x4, 16x16; staged=1 with chunk 32 and the
+ * same tiles.
  */
 typedef struct sarbp_tuning {
     int32_t chunk;        /* pulses per chunk: 32 or 64                       */

@@ -96,12 +96,20 @@ bool build_params(const sarbp_scene *s, SceneParams *p)
     return true;
 }
 
-static bool valid_tuning(sarbp_tuning *t)
+// Library default: the TMA-staged kernel, 32-pulse chunks, 16 x 16 pixel
+// tiles (fastest measured on the 4000 x 250 / 40001-pulse workload).
+bool valid_tuning(sarbp_tuning *t)
 {
-    if (t->chunk == 0) t->chunk = 64;
+    if (t->chunk == 0 && t->tile0 == 0 && t->tile1 == 0 && t->staged == 0) {
+        t->chunk = 32;
+        t->tile0 = 16;
+        t->tile1 = 16;
+        t->staged = 1;
+    }
+    if (t->chunk == 0) t->chunk = 32;
     if (t->tile0 == 0 && t->tile1 == 0) {
-        t->tile0 = 32;
-        t->tile1 = 8;
+        t->tile0 = 16;
+        t->tile1 = 16;
     }
     if (t->chunk != 32 && t->chunk != 64) {
         set_error("tuning.chunk must be 32 or 64 (got %d)", t->chunk);

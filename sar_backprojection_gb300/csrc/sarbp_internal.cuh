@@ -105,6 +105,7 @@ namespace sarbp {
 void set_error(const char *fmt, ...);
 bool build_params(const sarbp_scene *s, SceneParams *p);
 int cuda_status(cudaError_t e, const char *what);
+bool valid_tuning(sarbp_tuning *t);   // fills library defaults, validates
 
 // Mixed-path workspace layout (offsets 256-byte aligned).
 struct MixedLayout {
