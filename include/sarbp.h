@@ -161,6 +161,30 @@ SARBP_API int sarbp_focus_mixed_prepared(const sarbp_scene *scene, const sarbp_t
                                          size_t workspace_bytes, void *stream);
 
 /*
+ * Mixed-precision focusing for callers that cannot allocate device memory.
+ * No counterpart in the reference: it exists for callers that only hold the
+ * device pointers of their inputs and outputs -- plugins inside applications
+ * whose memory pool owns the device, real-time pipelines that may not call
+ * cudaMalloc (it can synchronise the device and has unbounded latency), thin
+ * bindings without an allocator.  Same arguments and results as
+ * sarbp_focus_mixed minus the workspace: the scratch lives in one
+ * library-owned device array of about 7 MiB, sized for scenes of at most
+ * SARBP_NOALLOC_MAX_PULSES pulses (larger scenes are rejected with
+ * SARBP_ERANGE), which every GPU that loads the library keeps until the
+ * process exits.  The first call on a device looks up the array's device
+ * address on that device, so make it before any stream capture.  Every call
+ * shares the one array: calls whose work overlaps on the GPU (different
+ * streams, or other host threads) race and must be serialised by the caller.
+ * Calls no cudaMalloc/cudaFree.
+ */
+#define SARBP_NOALLOC_MAX_PULSES 131072
+SARBP_API int sarbp_focus_mixed_noalloc(const sarbp_scene *scene,
+                                        const sarbp_tuning *tuning,
+                                        double *out, int32_t *nvalid,
+                                        uint64_t *checksum, uint64_t *counters,
+                                        void *stream);
+
+/*
  * Measurement helper (no counterpart in the reference, which publishes no
  * roofline): measures this device's issue rates with probe kernels on
  * `stream` and returns them in rates[0..3] = FP32 FMA lanes/s, SFU sin

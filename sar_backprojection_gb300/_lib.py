@@ -74,6 +74,8 @@ SIGNATURES = {
     "sarbp_focus_mixed_prepared": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, _P, _P,
                                              _P, _P, C.c_size_t, _P]),
     "sarbp_probe_issue_rates": (C.c_int, [C.POINTER(C.c_double), _P]),
+    "sarbp_focus_mixed_noalloc": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, _P, _P,
+                                            _P, _P]),
 }
 
 _lock = threading.Lock()
