@@ -457,6 +457,7 @@ def run_ours(args, dist: Dist):
                          "rel_l2": q["rel_l2"], "bins_bit_exact": bins_exact,
                          "ambiguous_bins_rederived": counters[_lib.CTR_AMBIGUOUS]}
                         if q else {"ambiguous_bins_rederived": counters[_lib.CTR_AMBIGUOUS]}),
+            "window_misses": counters[_lib.CTR_WINDOW_MISS],
             "latency": lat,
             "roofline": {"bound": "fp32_sfu_issue", "achieved": achieved, "peak": peak,
                          "unit": UNIT, "frac": achieved / peak, "traffic": traffic,

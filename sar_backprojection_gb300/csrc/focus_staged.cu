@@ -53,6 +53,47 @@ __device__ __forceinline__ void staged_tile_pixel(int t, int64_t tile0, int64_t 
     i1 = tile1 * T1 + (w / (T0 / 8)) * 4 + (lane >> 3);
 }
 
+// FP32 per-pulse range geometry: D = R^2 - R0^2, dR = R - R0, the window
+// column of the FP32 range bin, and whether that bin is within the tie band.
+__device__ __forceinline__ void pulse_eval(const ChunkSetup &S, float4 e, float inv_dra,
+                                           int colbias, float tie, float &D, float &dR,
+                                           int &col, bool &amb)
+{
+    D = fmaf(S.mx, e.x, fmaf(S.my, e.y, fmaf(S.mz, e.z, e.w)));
+    dR = D * fmaf(fmaf(S.c3, D, S.c2), D, S.c1);
+    const float g = fmaf(dR, inv_dra, S.g0);
+    const float t = __fadd_rn(g, 12582912.0f);
+    col = __float_as_int(t) + colbias;
+    amb = fabsf(__fsub_rn(g, __fsub_rn(t, 12582912.0f))) > tie;
+}
+
+// R^2 * exp(-j*dphi) as (wc, ws): term = (vx + j*vy) * (wc - j*ws).
+__device__ __forceinline__ void pulse_phasor(const ChunkSetup &S, float D, float dR, float beta,
+                                             float &wc, float &ws)
+{
+    const float ph = dR * fmaf(beta, dR, S.a);
+    float sn, cn;
+    __sincosf(ph, &sn, &cn);
+    const float w = S.r0sq + D;
+    wc = w * cn;
+    ws = w * sn;
+}
+
+// Setup of a lane without work in this chunk: every pulse maps to column 0.
+__device__ __forceinline__ void safe_setup(ChunkSetup &S, int b0)
+{
+    S.mx = S.my = S.mz = 0.f;
+    S.c1 = S.c2 = S.c3 = 0.f;
+    S.g0 = 0.f;
+    S.a = 0.f;
+    S.r0sq = 0.f;
+    S.w0re = 1.f;
+    S.w0im = 0.f;
+    S.eps = 0.f;
+    S.n0 = b0;
+    S.exact = false;
+}
+
 template <int CHUNK, int T0, int T1, int W, bool kChecksum>
 __global__ void __launch_bounds__(T0 *T1)
 focus_mixed_staged_kernel(const SceneParams P, const __grid_constant__ CUtensorMap raw_map,
@@ -178,75 +219,146 @@ focus_mixed_staged_kernel(const SceneParams P, const __grid_constant__ CUtensorM
                 const int64_t K = c * CHUNK;
                 const int jmin = (int)(lo > K ? lo - K : 0);
                 const int jmax = (int)(hi < K + CHUNK - 1 ? hi - K : CHUNK - 1);
-                if (ready && active && jmin <= jmax) {
+                const bool work = ready && active && jmin <= jmax;
+                const float2 *sraw =
+                    reinterpret_cast<const float2 *>(smem + (size_t)s * SM::stage_bytes);
+                const float4 *stab = reinterpret_cast<const float4 *>(
+                    smem + (size_t)s * SM::stage_bytes + SM::raw_bytes);
+                const int b0 = window_start(q);
+                // window covers every bin the tile can reach and lies inside
+                // the kept bins 0..nra-2: no per-pulse validity/window tests
+                const bool win_ok = s_wlo[q] >= 0 && (int64_t)s_whi[q] <= P.nra - 2 &&
+                                    s_whi[q] - b0 < W;
+                ChunkSetup S;
+                safe_setup(S, b0);                 // lanes without work read column 0
+                if (work) {
                     ++chunks;
-                    const float2 *sraw =
-                        reinterpret_cast<const float2 *>(smem + (size_t)s * SM::stage_bytes);
-                    const float4 *stab = reinterpret_cast<const float4 *>(
-                        smem + (size_t)s * SM::stage_bytes + SM::raw_bytes);
-                    const int b0 = window_start(q);
                     ChunkRef ref;
                     ref.emax = __ldg(&ctab[c].emax);
                     ref.thi = __ldg(&ctab[c].thi);
                     ref.tlo = __ldg(&ctab[c].tlo);
-                    ChunkSetup S;
                     chunk_setup(P, pf, ref, S);
-                    if (S.exact) {
-                        const double px = P.x[ii], py = P.y[ii], pz = P.z[ii];
-                        double sre = 0.0, sim = 0.0;
-                        for (int j = jmin; j <= jmax; ++j) {
-                            int64_t bin;
-                            double tre, tim;
-                            if (exact_term(P, px, py, pz, K + j, &bin, &tre, &tim)) {
-                                sre += tre;
-                                sim += tim;
-                                ++n;
-                                if (kChecksum) cs += mix64(K + j, bin);
-                            }
+                }
+                const bool exact = work && S.exact;
+                const bool fast = __all_sync(0xffffffffu, !work || (jmin == 0 &&
+                                                                    jmax == CHUNK - 1 &&
+                                                                    win_ok && !exact));
+                if (exact) {
+                    const double px = P.x[ii], py = P.y[ii], pz = P.z[ii];
+                    double sre = 0.0, sim = 0.0;
+                    for (int j = jmin; j <= jmax; ++j) {
+                        int64_t bin;
+                        double tre, tim;
+                        if (exact_term(P, px, py, pz, K + j, &bin, &tre, &tim)) {
+                            sre += tre;
+                            sim += tim;
+                            ++n;
+                            if (kChecksum) cs += mix64(K + j, bin);
                         }
-                        kahan_add(acc_re, cmp_re, (float)sre);
-                        kahan_add(acc_im, cmp_im, (float)sim);
+                    }
+                    kahan_add(acc_re, cmp_re, (float)sre);
+                    kahan_add(acc_im, cmp_im, (float)sim);
+                } else {
+                    const int colbias = S.n0 - b0 - 0x4B400000;
+                    const float tie = 0.5f - S.eps;
+                    float sre = 0.f, sim = 0.f;
+                    uint32_t amb_mask = 0, miss_mask = 0, valid_mask;
+                    if (fast) {
+                        valid_mask = 0xffffffffu;
+#pragma unroll
+                        for (int j = 0; j < CHUNK; ++j) {
+                            float D, dR;
+                            int col;
+                            bool amb;
+                            pulse_eval(S, stab[j], P.inv_dra_f, colbias, tie, D, dR, col, amb);
+                            if (amb) amb_mask |= 1u << j;
+                            col = (int)min((unsigned)col, (unsigned)(W - 1));
+                            const float2 v = sraw[j * W + col];
+                            float wc, ws;
+                            pulse_phasor(S, D, dR, P.beta_f, wc, ws);
+                            sre = fmaf(v.x, wc, fmaf(v.y, ws, sre));
+                            sim = fmaf(v.y, wc, fmaf(-v.x, ws, sim));
+                            if (kChecksum) cs += mix64(K + j, col + b0);
+                        }
                     } else {
+                        valid_mask = 0;
+                        const uint32_t apmask =
+                            work ? (((jmax == 31) ? 0xffffffffu : ((1u << (jmax + 1)) - 1u)) &
+                                    ~((1u << jmin) - 1u))
+                                 : 0u;
+#pragma unroll
+                        for (int j = 0; j < CHUNK; ++j) {
+                            float D, dR;
+                            int col;
+                            bool amb;
+                            pulse_eval(S, stab[j], P.inv_dra_f, colbias, tie, D, dR, col, amb);
+                            const bool inap = (apmask >> j) & 1u;
+                            const int bin = col + b0;
+                            const bool ok = inap && (unsigned)bin < nra_m1;
+                            const bool inw = (unsigned)col < (unsigned)W;
+                            float2 v = make_float2(0.f, 0.f);
+                            if (ok && inw) v = sraw[j * W + col];
+                            if (ok) valid_mask |= 1u << j;
+                            if (ok && !inw) miss_mask |= 1u << j;
+                            if (inap && amb) amb_mask |= 1u << j;
+                            float wc, ws;
+                            pulse_phasor(S, D, dR, P.beta_f, wc, ws);
+                            sre = fmaf(v.x, wc, fmaf(v.y, ws, sre));
+                            sim = fmaf(v.y, wc, fmaf(-v.x, ws, sim));
+                            if (kChecksum && ok) cs += mix64(K + j, bin);
+                        }
+                    }
+                    if (work) {
+                        // rare fix-ups: ties re-derived exactly, window misses from L2
+                        uint32_t fix = amb_mask | miss_mask;
                         const float2 *rowc = P.raw + K * P.pitch;
-                        const float tie = 0.5f - S.eps;
-                        const int nb0 = S.n0 - b0;
-                        float sre = 0.f, sim = 0.f;
-#pragma unroll 4
-                        for (int j = jmin; j <= jmax; ++j) {
-                            const float4 e = stab[j];
-                            const float D = fmaf(S.mx, e.x, fmaf(S.my, e.y, fmaf(S.mz, e.z, e.w)));
-                            const float dR = D * fmaf(fmaf(S.c3, D, S.c2), D, S.c1);
-                            const float g = fmaf(dR, P.inv_dra_f, S.g0);
-                            int ib;
-                            const float gr = round_shift(g, ib);
-                            int col = nb0 + ib;              // bin - b0
-                            if (fabsf(__fsub_rn(g, gr)) > tie) {
-                                col = resolve_bin(P, pf, ii, pff, K + j);
-                                col = col < 0 ? INT_MIN / 2 : col - b0;
+                        while (fix) {
+                            const int j = __ffs(fix) - 1;
+                            fix &= fix - 1;
+                            float D, dR;
+                            int col;
+                            bool amb;
+                            pulse_eval(S, stab[j], P.inv_dra_f, colbias, tie, D, dR, col, amb);
+                            int bin_old = col + b0;
+                            bool ok_old;
+                            float2 v_old = make_float2(0.f, 0.f);
+                            if (fast) {
+                                col = (int)min((unsigned)col, (unsigned)(W - 1));
+                                bin_old = col + b0;
+                                ok_old = true;
+                                v_old = sraw[j * W + col];
+                            } else {
+                                ok_old = (unsigned)bin_old < nra_m1;
+                                if (ok_old && (unsigned)col < (unsigned)W) v_old = sraw[j * W + col];
+                            }
+                            int bin = bin_old;
+                            if ((amb_mask >> j) & 1u) {
+                                bin = resolve_bin(P, pf, ii, pff, K + j);
                                 ++ambiguous;
                             }
-                            const int bin = col + b0;
-                            const bool ok = (unsigned)bin < nra_m1;
-                            float2 v = make_float2(0.f, 0.f);
-                            if (ok) {
-                                if ((unsigned)col < (unsigned)W) {
-                                    v = sraw[j * W + col];
+                            const bool ok_new = bin >= 0 && (unsigned)bin < nra_m1;
+                            float2 v_new = make_float2(0.f, 0.f);
+                            if (ok_new) {
+                                const int cn = bin - b0;
+                                if ((unsigned)cn < (unsigned)W) {
+                                    v_new = sraw[j * W + cn];
                                 } else {
-                                    v = __ldg(rowc + (j * pitch + bin));
+                                    v_new = __ldg(rowc + (j * pitch + bin));
                                     ++misses;
                                 }
                             }
-                            const float ph = dR * fmaf(P.beta_f, dR, S.a);
-                            float sn, cn;
-                            __sincosf(ph, &sn, &cn);
-                            const float tre = fmaf(v.x, cn, v.y * sn);
-                            const float tim = fmaf(v.y, cn, -(v.x * sn));
-                            const float w = S.r0sq + D;
-                            sre = fmaf(w, tre, sre);
-                            sim = fmaf(w, tim, sim);
-                            n += ok ? 1 : 0;
-                            if (kChecksum && ok) cs += mix64(K + j, bin);
+                            float wc, ws;
+                            pulse_phasor(S, D, dR, P.beta_f, wc, ws);
+                            const float dx = v_new.x - v_old.x, dy = v_new.y - v_old.y;
+                            sre = fmaf(dx, wc, fmaf(dy, ws, sre));
+                            sim = fmaf(dy, wc, fmaf(-dx, ws, sim));
+                            valid_mask = ok_new ? (valid_mask | (1u << j)) : (valid_mask & ~(1u << j));
+                            if (kChecksum) {
+                                if (ok_old) cs -= mix64(K + j, bin_old);
+                                if (ok_new) cs += mix64(K + j, bin);
+                            }
                         }
+                        n += __popc(valid_mask);
                         const float rre = fmaf(sre, S.w0re, -(sim * S.w0im));
                         const float rim = fmaf(sre, S.w0im, sim * S.w0re);
                         kahan_add(acc_re, cmp_re, rre);
