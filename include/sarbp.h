@@ -72,17 +72,18 @@ typedef struct sarbp_scene {
 
 /*
  * Tuning of the mixed-precision kernel.  An all-zero struct (or NULL) selects
- * the library default (TMA-staged, 32-pulse chunks, 16 x 16 pixel tiles);
- * sarbp_default_tuning() fills the defaults explicitly.  Supported: staged=0
- * with chunk 32/64 and tiles 32x8, 64x4, 16x16; staged=1 with chunk 32 and the
- * same tiles.
+ * the library default; sarbp_default_tuning() fills the defaults explicitly.
+ * Supported: staged=0 with chunk 32/64 and tiles 32x8, 64x4, 16x16; staged=1
+ * with chunk 32 and (tile, window) 16x16/128, 16x16/160, 16x8/128, 32x8/128,
+ * 64x4/128.
  */
 typedef struct sarbp_tuning {
     int32_t chunk;        /* pulses per chunk: 32 or 64                       */
     int32_t tile0;        /* pixel-tile extent along dim0 (power of two)      */
     int32_t tile1;        /* pixel-tile extent along dim1                     */
     int32_t staged;       /* 1: TMA-staged shared-memory raw window, 0: L1/L2 gathers */
-    int32_t reserved[4];
+    int32_t window;       /* staged: range bins staged per pulse chunk (0: default) */
+    int32_t reserved[3];
 } sarbp_tuning;
 
 /* Device counters written by the mixed kernel when `counters` is non-NULL. */
@@ -159,6 +160,43 @@ SARBP_API int sarbp_focus_mixed_prepared(const sarbp_scene *scene, const sarbp_t
                                          double *out, int32_t *nvalid, uint64_t *checksum,
                                          uint64_t *counters, void *workspace,
                                          size_t workspace_bytes, void *stream);
+
+/*
+ * Batches: many scenes of uneven size in one persistent launch.
+ * Replaces the reference's per-batch host loops (gpu_small_dataset.py:285-339,
+ * main_gpu.py:415-586), which launch one kernel per pixel batch and copy
+ * results back after each; here all scenes' pixel tiles are items of one
+ * device work queue, drained by a persistent grid (one launch, capturable in
+ * a CUDA graph).
+ *
+ * sarbp_tile_count / sarbp_tile_costs: number of pixel tiles of a scene under
+ *   `tuning`, and per tile (device int64 array) the sum of its pixels' kept
+ *   aperture lengths -- the cost estimate used to order the queue.
+ * sarbp_batch_workspace_size: bytes of the batch workspace (scene
+ *   descriptors + queue) for `nscenes` scenes and up to `max_items` items.
+ * sarbp_batch_set_scene: describe scene `slot` (its mixed workspace must be
+ *   prepared with sarbp_mixed_prepare under the same tuning).
+ * sarbp_batch_set_items: upload the queue, `n_items` (scene slot, tile index)
+ *   int32 pairs in processing order (decreasing cost balances the load).
+ * sarbp_batch_focus: reset the queue cursor and launch the persistent kernel;
+ *   stream-ordered, no host synchronisation, capturable in a CUDA graph.
+ *   `diagnostics` != 0 also writes the scenes' checksum outputs.
+ * The batch path needs the staged kernel (tuning.staged = 1, chunk 32).
+ */
+SARBP_API int64_t sarbp_tile_count(const sarbp_scene *scene, const sarbp_tuning *tuning);
+SARBP_API int sarbp_tile_costs(const sarbp_scene *scene, const sarbp_tuning *tuning,
+                               int64_t *costs, void *stream);
+SARBP_API int64_t sarbp_batch_workspace_size(int32_t nscenes, int64_t max_items);
+SARBP_API int sarbp_batch_set_scene(void *batch_ws, size_t batch_bytes, int32_t nscenes,
+                                    int32_t slot, const sarbp_scene *scene,
+                                    const sarbp_tuning *tuning, void *scene_ws,
+                                    size_t scene_ws_bytes, double *out, int32_t *nvalid,
+                                    uint64_t *checksum, void *stream);
+SARBP_API int sarbp_batch_set_items(void *batch_ws, size_t batch_bytes, int32_t nscenes,
+                                    const int32_t *items, int64_t n_items, void *stream);
+SARBP_API int sarbp_batch_focus(void *batch_ws, size_t batch_bytes, int32_t nscenes,
+                                const sarbp_tuning *tuning, int64_t n_items, int32_t diagnostics,
+                                uint64_t *counters, void *stream);
 
 /*
  * Mixed-precision focusing for callers that cannot allocate device memory.

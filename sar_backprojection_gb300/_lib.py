@@ -52,12 +52,12 @@ class Tuning(C.Structure):
 
     _fields_ = [
         ("chunk", C.c_int32), ("tile0", C.c_int32), ("tile1", C.c_int32),
-        ("staged", C.c_int32), ("reserved", C.c_int32 * 4),
+        ("staged", C.c_int32), ("window", C.c_int32), ("reserved", C.c_int32 * 3),
     ]
 
     def as_dict(self) -> dict:
         return {"chunk": self.chunk, "tile0": self.tile0, "tile1": self.tile1,
-                "staged": self.staged}
+                "staged": self.staged, "window": self.window}
 
 
 _P = C.c_void_p
@@ -76,6 +76,14 @@ SIGNATURES = {
     "sarbp_probe_issue_rates": (C.c_int, [C.POINTER(C.c_double), _P]),
     "sarbp_focus_mixed_noalloc": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, _P, _P,
                                             _P, _P]),
+    "sarbp_tile_count": (C.c_int64, [C.POINTER(Scene), C.POINTER(Tuning)]),
+    "sarbp_tile_costs": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, _P]),
+    "sarbp_batch_workspace_size": (C.c_int64, [C.c_int32, C.c_int64]),
+    "sarbp_batch_set_scene": (C.c_int, [_P, C.c_size_t, C.c_int32, C.c_int32, C.POINTER(Scene),
+                                        C.POINTER(Tuning), _P, C.c_size_t, _P, _P, _P, _P]),
+    "sarbp_batch_set_items": (C.c_int, [_P, C.c_size_t, C.c_int32, _P, C.c_int64, _P]),
+    "sarbp_batch_focus": (C.c_int, [_P, C.c_size_t, C.c_int32, C.POINTER(Tuning), C.c_int64,
+                                    C.c_int32, _P, _P]),
 }
 
 _lock = threading.Lock()

@@ -111,6 +111,7 @@ bool valid_tuning(sarbp_tuning *t)
         t->tile0 = 16;
         t->tile1 = 16;
     }
+    if (t->staged && t->window == 0) t->window = 128;
     if (t->chunk != 32 && t->chunk != 64) {
         set_error("tuning.chunk must be 32 or 64 (got %d)", t->chunk);
         return false;
@@ -219,6 +220,75 @@ SARBP_API int sarbp_focus_mixed(const sarbp_scene *scene, const sarbp_tuning *tu
     if (rc) return rc;
     return launch_mixed_main(P, T, workspace, workspace_bytes, out, nvalid, checksum, counters,
                              s);
+}
+
+SARBP_API int64_t sarbp_tile_count(const sarbp_scene *scene, const sarbp_tuning *tuning)
+{
+    SceneParams P;
+    sarbp_tuning T;
+    int rc = mixed_args(scene, tuning, &P, &T);
+    if (rc) return rc;
+    int64_t nt = 0;
+    rc = tile_count(P, T, &nt);
+    return rc ? rc : nt;
+}
+
+SARBP_API int sarbp_tile_costs(const sarbp_scene *scene, const sarbp_tuning *tuning,
+                               int64_t *costs, void *stream)
+{
+    SceneParams P;
+    sarbp_tuning T;
+    int rc = mixed_args(scene, tuning, &P, &T);
+    if (rc) return rc;
+    if (!costs) {
+        set_error("sarbp_tile_costs: costs is NULL");
+        return SARBP_EINVAL;
+    }
+    return tile_costs(P, T, costs, static_cast<cudaStream_t>(stream));
+}
+
+SARBP_API int64_t sarbp_batch_workspace_size(int32_t nscenes, int64_t max_items)
+{
+    g_last_error[0] = 0;
+    if (nscenes <= 0 || max_items < 0) {
+        set_error("sarbp_batch_workspace_size: nscenes must be positive");
+        return SARBP_EINVAL;
+    }
+    return batch_workspace_size(nscenes, max_items);
+}
+
+SARBP_API int sarbp_batch_set_scene(void *batch_ws, size_t batch_bytes, int32_t nscenes,
+                                    int32_t slot, const sarbp_scene *scene,
+                                    const sarbp_tuning *tuning, void *scene_ws,
+                                    size_t scene_ws_bytes, double *out, int32_t *nvalid,
+                                    uint64_t *checksum, void *stream)
+{
+    SceneParams P;
+    sarbp_tuning T;
+    int rc = mixed_args(scene, tuning, &P, &T);
+    if (rc) return rc;
+    return batch_set_scene(batch_ws, batch_bytes, slot, nscenes, P, T, scene_ws, scene_ws_bytes,
+                           out, nvalid, checksum, static_cast<cudaStream_t>(stream));
+}
+
+SARBP_API int sarbp_batch_set_items(void *batch_ws, size_t batch_bytes, int32_t nscenes,
+                                    const int32_t *items, int64_t n_items, void *stream)
+{
+    g_last_error[0] = 0;
+    return batch_set_items(batch_ws, batch_bytes, nscenes, items, n_items,
+                           static_cast<cudaStream_t>(stream));
+}
+
+SARBP_API int sarbp_batch_focus(void *batch_ws, size_t batch_bytes, int32_t nscenes,
+                                const sarbp_tuning *tuning, int64_t n_items, int32_t diagnostics,
+                                uint64_t *counters, void *stream)
+{
+    g_last_error[0] = 0;
+    sarbp_tuning T{};
+    if (tuning) T = *tuning;
+    if (!valid_tuning(&T)) return SARBP_EINVAL;
+    return batch_focus(batch_ws, batch_bytes, nscenes, T, n_items, diagnostics != 0, counters,
+                       static_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

@@ -21,8 +21,10 @@
 // All mbarrier waits are bounded; a wait that gives up marks the workspace
 // status block and the CTA leaves after its last copy lands (or after a
 // second bounded wait).
+#include <algorithm>
 #include <climits>
 #include <cstdio>
+#include <cstring>
 
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -94,26 +96,63 @@ __device__ __forceinline__ void safe_setup(ChunkSetup &S, int b0)
     S.exact = false;
 }
 
+// Shared-memory state of one CTA of a staged kernel.  It persists across the
+// tiles a persistent CTA processes: the stage counter keeps the mbarrier
+// phases in step.
+struct StagedCta {
+    unsigned char *smem;       // 2 stages, 1024-byte aligned
+    uint64_t *full_bar;        // [2] copy-completion barriers
+    int *s_wlo, *s_whi;        // [kMaxPassChunks] range windows of a pass
+    long long *s_lo, *s_hi;    // tile-wide pulse range
+    uint32_t it;               // chunk iteration counter (stage = it & 1)
+    bool pending[2];           // thread 0: copies in flight per stage
+    uint32_t pending_parity[2];
+};
+
+struct TileTables {
+    const float4 *ptab;
+    const PulseFF *pff;
+    const ChunkRef *ctab;
+};
+
+struct TileOutputs {
+    double2 *out;
+    int32_t *nvalid;
+    uint64_t *checksum;
+};
+
+struct TileStats {
+    unsigned ambiguous, chunks, misses;
+};
+
+// One scene of a batch, as the persistent kernel reads it from device memory.
+struct BatchScene {
+    CUtensorMap map;          // raw-data window tensor map (64-byte aligned)
+    SceneParams P;
+    TileTables tables;
+    TileOutputs outputs;
+    int64_t ntile0, ntiles;
+};
+
+// Focus one pixel tile; false if a bounded wait gave up (the CTA must stop).
+// Every thread of the CTA calls it with the same tile.
 template <int CHUNK, int T0, int T1, int W, bool kChecksum>
-__global__ void __launch_bounds__(T0 *T1)
-focus_mixed_staged_kernel(const SceneParams P, const __grid_constant__ CUtensorMap raw_map,
-                          const float4 *__restrict__ ptab, const PulseFF *__restrict__ pff,
-                          const ChunkRef *__restrict__ ctab, int64_t ntile0,
-                          double2 *__restrict__ out, int32_t *__restrict__ nvalid,
-                          uint64_t *__restrict__ checksum,
-                          unsigned long long *__restrict__ counters, StatusBlock *status)
+__device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P,
+                                            const CUtensorMap *raw_map, const TileTables &tb,
+                                            int64_t tile0, int64_t tile1, const TileOutputs &o,
+                                            TileStats &st)
 {
     using SM = StagedSmem<CHUNK, W>;
-    extern __shared__ unsigned char smem_dyn[];
-    unsigned char *smem = reinterpret_cast<unsigned char *>(
-        (reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~(uintptr_t)1023);
-    __shared__ __align__(8) uint64_t full_bar[2];
-    __shared__ int s_wlo[kMaxPassChunks], s_whi[kMaxPassChunks];
-    __shared__ long long s_lo, s_hi;
+    unsigned char *smem = cta.smem;
+    uint64_t *full_bar = cta.full_bar;
+    int *s_wlo = cta.s_wlo, *s_whi = cta.s_whi;
+    const float4 *ptab = tb.ptab;
+    const PulseFF *pff = tb.pff;
+    const ChunkRef *ctab = tb.ctab;
 
     const int t = threadIdx.x;
     int64_t i0, i1;
-    staged_tile_pixel<T0, T1>(t, blockIdx.x % ntile0, blockIdx.x / ntile0, i0, i1);
+    staged_tile_pixel<T0, T1>(t, tile0, tile1, i0, i1);
     const bool inside = i0 < P.dim0 && i1 < P.dim1;
     const int64_t ii = inside ? i0 + P.dim0 * i1 : 0;
     int64_t lo = 0, hi = -1;
@@ -121,19 +160,16 @@ focus_mixed_staged_kernel(const SceneParams P, const __grid_constant__ CUtensorM
         inside && pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi);
 
     if (t == 0) {
-        s_lo = LLONG_MAX;
-        s_hi = -1;
-        mbar_init(&full_bar[0], 1);
-        mbar_init(&full_bar[1], 1);
-        mbar_fence_init();
+        *cta.s_lo = LLONG_MAX;
+        *cta.s_hi = -1;
     }
     __syncthreads();
     if (active) {
-        atomicMin(&s_lo, (long long)lo);
-        atomicMax(&s_hi, (long long)hi);
+        atomicMin(cta.s_lo, (long long)lo);
+        atomicMax(cta.s_hi, (long long)hi);
     }
     __syncthreads();
-    const int64_t tlo = s_lo, thi = s_hi;
+    const int64_t tlo = *cta.s_lo, thi = *cta.s_hi;
 
     PixelFF pf{};
     if (active) pf = pixel_ff(P.x[ii], P.y[ii], P.z[ii]);
@@ -143,11 +179,10 @@ focus_mixed_staged_kernel(const SceneParams P, const __grid_constant__ CUtensorM
     unsigned ambiguous = 0, chunks = 0, misses = 0;
     const unsigned nra_m1 = (unsigned)(P.nra - 1);
     const int pitch = (int)P.pitch;
-    uint32_t it = 0;             // chunk iteration counter across passes (stage = it & 1)
-    bool pending[2] = {false, false};     // thread 0: copies in flight per stage
-    uint32_t pending_parity[2] = {0, 0};
+    uint32_t &it = cta.it;
+    bool *pending = cta.pending;
+    uint32_t *pending_parity = cta.pending_parity;
     bool aborted = false;
-
     if (thi >= 0) {
         const int64_t c_first = tlo / CHUNK, c_last = thi / CHUNK;
         for (int64_t cb = c_first; cb <= c_last && !aborted; cb += kMaxPassChunks) {
@@ -203,7 +238,7 @@ focus_mixed_staged_kernel(const SceneParams P, const __grid_constant__ CUtensorM
                 unsigned char *base = smem + (size_t)s * SM::stage_bytes;
                 const int64_t K = (cb + q) * CHUNK;
                 mbar_arrive_expect_tx(&full_bar[s], (uint32_t)SM::stage_bytes);
-                tma_load_2d(base, &raw_map, &full_bar[s], window_start(q), (int)K);
+                tma_load_2d(base, raw_map, &full_bar[s], window_start(q), (int)K);
                 bulk_load(base + SM::raw_bytes, ptab + K, (uint32_t)SM::tab_bytes, &full_bar[s]);
                 pending[s] = true;
                 pending_parity[s] = use & 1;
@@ -278,7 +313,7 @@ focus_mixed_staged_kernel(const SceneParams P, const __grid_constant__ CUtensorM
                             pulse_phasor(S, D, dR, P.beta_f, wc, ws);
                             sre = fmaf(v.x, wc, fmaf(v.y, ws, sre));
                             sim = fmaf(v.y, wc, fmaf(-v.x, ws, sim));
-                            if (kChecksum) cs += mix64(K + j, col + b0);
+                            if (kChecksum && work) cs += mix64(K + j, col + b0);
                         }
                     } else {
                         valid_mask = 0;
@@ -374,18 +409,10 @@ focus_mixed_staged_kernel(const SceneParams P, const __grid_constant__ CUtensorM
         }
     }
 
-    if (aborted) {
-        if (t == 0) {
-            atomicOr(&status->error, 1u);
-            atomicExch(&status->where, 1u);
-            // let copies still in flight land before the CTA's shared memory goes
-            for (int s = 0; s < 2; ++s)
-                if (pending[s]) mbar_wait(&full_bar[s], pending_parity[s], kWaitLimit);
-            if (counters) atomicAdd(counters + SARBP_CTR_TIMEOUTS, 1ull);
-        }
-        return;
-    }
-
+    st.ambiguous += ambiguous;
+    st.chunks += chunks;
+    st.misses += misses;
+    if (aborted) return false;
     if (inside) {
         double2 res = make_double2(0.0, 0.0);
         if (n > 0) {
@@ -393,22 +420,122 @@ focus_mixed_staged_kernel(const SceneParams P, const __grid_constant__ CUtensorM
             res = make_double2(((double)acc_re - (double)cmp_re) * inv,
                                ((double)acc_im - (double)cmp_im) * inv);
         }
-        out[ii] = res;
-        if (nvalid) nvalid[ii] = n;
-        if (kChecksum) checksum[ii] = cs;
+        o.out[ii] = res;
+        if (o.nvalid) o.nvalid[ii] = n;
+        if (kChecksum) o.checksum[ii] = cs;
     }
-    if (counters) {
-        for (int o = 16; o > 0; o >>= 1) {
-            ambiguous += __shfl_xor_sync(0xffffffffu, ambiguous, o);
-            chunks += __shfl_xor_sync(0xffffffffu, chunks, o);
-            misses += __shfl_xor_sync(0xffffffffu, misses, o);
-        }
-        if ((t & 31) == 0) {
-            if (ambiguous) atomicAdd(counters + SARBP_CTR_AMBIGUOUS, (unsigned long long)ambiguous);
-            if (chunks) atomicAdd(counters + SARBP_CTR_CHUNKS, (unsigned long long)chunks);
-            if (misses) atomicAdd(counters + SARBP_CTR_WINDOW_MISS, (unsigned long long)misses);
+    return true;
+}
+
+template <int CHUNK, int W>
+__device__ __forceinline__ StagedCta staged_cta_init(unsigned char *smem_dyn, uint64_t *full_bar,
+                                                     int *s_wlo, int *s_whi, long long *s_lo,
+                                                     long long *s_hi)
+{
+    StagedCta cta;
+    cta.smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~(uintptr_t)1023);
+    cta.full_bar = full_bar;
+    cta.s_wlo = s_wlo;
+    cta.s_whi = s_whi;
+    cta.s_lo = s_lo;
+    cta.s_hi = s_hi;
+    cta.it = 0;
+    cta.pending[0] = cta.pending[1] = false;
+    cta.pending_parity[0] = cta.pending_parity[1] = 0;
+    if (threadIdx.x == 0) {
+        mbar_init(&full_bar[0], 1);
+        mbar_init(&full_bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    return cta;
+}
+
+// A bounded wait gave up: mark the status block and let copies still in
+// flight land before the CTA's shared memory goes away.
+__device__ __forceinline__ void staged_abort(StagedCta &cta, StatusBlock *status,
+                                             unsigned long long *counters)
+{
+    if (threadIdx.x == 0) {
+        atomicOr(&status->error, 1u);
+        atomicExch(&status->where, 1u);
+        for (int s = 0; s < 2; ++s)
+            if (cta.pending[s]) mbar_wait(&cta.full_bar[s], cta.pending_parity[s], kWaitLimit);
+        if (counters) atomicAdd(counters + SARBP_CTR_TIMEOUTS, 1ull);
+    }
+}
+
+__device__ __forceinline__ void flush_stats(TileStats &st, unsigned long long *counters)
+{
+    if (!counters) return;
+    for (int o = 16; o > 0; o >>= 1) {
+        st.ambiguous += __shfl_xor_sync(0xffffffffu, st.ambiguous, o);
+        st.chunks += __shfl_xor_sync(0xffffffffu, st.chunks, o);
+        st.misses += __shfl_xor_sync(0xffffffffu, st.misses, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (st.ambiguous)
+            atomicAdd(counters + SARBP_CTR_AMBIGUOUS, (unsigned long long)st.ambiguous);
+        if (st.chunks) atomicAdd(counters + SARBP_CTR_CHUNKS, (unsigned long long)st.chunks);
+        if (st.misses) atomicAdd(counters + SARBP_CTR_WINDOW_MISS, (unsigned long long)st.misses);
+    }
+}
+
+// One scene: one CTA per pixel tile.
+template <int CHUNK, int T0, int T1, int W, bool kChecksum>
+__global__ void __launch_bounds__(T0 *T1)
+focus_mixed_staged_kernel(const SceneParams P, const __grid_constant__ CUtensorMap raw_map,
+                          const TileTables tb, int64_t ntile0, const TileOutputs o,
+                          unsigned long long *__restrict__ counters, StatusBlock *status)
+{
+    extern __shared__ unsigned char smem_dyn[];
+    __shared__ __align__(8) uint64_t full_bar[2];
+    __shared__ int s_wlo[kMaxPassChunks], s_whi[kMaxPassChunks];
+    __shared__ long long s_lo, s_hi;
+    StagedCta cta = staged_cta_init<CHUNK, W>(smem_dyn, full_bar, s_wlo, s_whi, &s_lo, &s_hi);
+    TileStats st{0, 0, 0};
+    const bool ok = staged_tile<CHUNK, T0, T1, W, kChecksum>(
+        cta, P, &raw_map, tb, blockIdx.x % ntile0, blockIdx.x / ntile0, o, st);
+    if (!ok) {
+        staged_abort(cta, status, counters);
+        return;
+    }
+    flush_stats(st, counters);
+}
+
+// Many scenes in one persistent launch: CTAs pull (scene, tile) work items
+// from a device queue (a list ordered by decreasing estimated cost and an
+// atomic cursor) until it is empty.
+template <int CHUNK, int T0, int T1, int W, bool kChecksum>
+__global__ void __launch_bounds__(T0 *T1, 3)
+focus_batch_staged_kernel(const BatchScene *__restrict__ scenes, const int2 *__restrict__ items,
+                          int64_t n_items, unsigned long long *cursor,
+                          unsigned long long *__restrict__ counters, StatusBlock *status)
+{
+    extern __shared__ unsigned char smem_dyn[];
+    __shared__ __align__(8) uint64_t full_bar[2];
+    __shared__ int s_wlo[kMaxPassChunks], s_whi[kMaxPassChunks];
+    __shared__ long long s_lo, s_hi;
+    __shared__ long long s_item[2];
+    StagedCta cta = staged_cta_init<CHUNK, W>(smem_dyn, full_bar, s_wlo, s_whi, &s_lo, &s_hi);
+    TileStats st{0, 0, 0};
+    for (int round = 0;; ++round) {
+        if (threadIdx.x == 0) s_item[round & 1] = (long long)atomicAdd(cursor, 1ull);
+        __syncthreads();
+        const long long item = s_item[round & 1];
+        if (item >= n_items) break;
+        const int2 w = items[item];
+        const BatchScene &B = scenes[w.x];
+        const int64_t tile = w.y;
+        const bool ok = staged_tile<CHUNK, T0, T1, W, kChecksum>(
+            cta, B.P, &B.map, B.tables, tile % B.ntile0, tile / B.ntile0, B.outputs, st);
+        if (!ok) {
+            staged_abort(cta, status, counters);
+            return;
         }
     }
+    flush_stats(st, counters);
 }
 
 // ---------------------------------------------------------------------------
@@ -460,6 +587,39 @@ static int make_raw_map(const SceneParams &P, int W, int chunk, CUtensorMap *map
 }
 
 template <int CHUNK, int T0, int T1, int W>
+static int ensure_smem_attr()
+{
+    using SM = StagedSmem<CHUNK, W>;
+    // per device: the attribute belongs to the function in each context
+    static bool done[64] = {};
+    int dev = 0;
+    int rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+    if (rc) return rc;
+    if (dev < 0 || dev >= 64 || done[dev]) return SARBP_OK;
+    const void *ks[4] = {(const void *)focus_mixed_staged_kernel<CHUNK, T0, T1, W, false>,
+                         (const void *)focus_mixed_staged_kernel<CHUNK, T0, T1, W, true>,
+                         (const void *)focus_batch_staged_kernel<CHUNK, T0, T1, W, false>,
+                         (const void *)focus_batch_staged_kernel<CHUNK, T0, T1, W, true>};
+    for (const void *k : ks) {
+        rc = cuda_status(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)SM::bytes),
+                         "staged smem attribute");
+        if (rc) return rc;
+    }
+    done[dev] = true;
+    return SARBP_OK;
+}
+
+static TileTables tables_of(char *ws, const MixedLayout &L)
+{
+    TileTables tb;
+    tb.ptab = reinterpret_cast<const float4 *>(ws + L.ptab);
+    tb.pff = reinterpret_cast<const PulseFF *>(ws + L.pff);
+    tb.ctab = reinterpret_cast<const ChunkRef *>(ws + L.ctab);
+    return tb;
+}
+
+template <int CHUNK, int T0, int T1, int W>
 int launch_staged_t(const SceneParams &P, const MixedLayout &L, char *ws, double *out,
                     int32_t *nvalid, uint64_t *checksum, uint64_t *counters, cudaStream_t stream)
 {
@@ -473,52 +633,215 @@ int launch_staged_t(const SceneParams &P, const MixedLayout &L, char *ws, double
     CUtensorMap map;
     int rc = make_raw_map(P, W, CHUNK, &map);
     if (rc) return rc;
-    auto *ptab = reinterpret_cast<const float4 *>(ws + L.ptab);
-    auto *pff = reinterpret_cast<const PulseFF *>(ws + L.pff);
-    auto *ctab = reinterpret_cast<const ChunkRef *>(ws + L.ctab);
+    rc = ensure_smem_attr<CHUNK, T0, T1, W>();
+    if (rc) return rc;
+    const TileTables tb = tables_of(ws, L);
+    const TileOutputs o{reinterpret_cast<double2 *>(out), nvalid, checksum};
     auto *status = reinterpret_cast<StatusBlock *>(ws + L.status);
     auto *ctr = reinterpret_cast<unsigned long long *>(counters);
-    auto *k_fast = focus_mixed_staged_kernel<CHUNK, T0, T1, W, false>;
-    auto *k_diag = focus_mixed_staged_kernel<CHUNK, T0, T1, W, true>;
-    static bool attr_done = false;
-    if (!attr_done) {
-        rc = cuda_status(cudaFuncSetAttribute(k_fast, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)SM::bytes),
-                         "staged smem attribute");
-        if (rc) return rc;
-        rc = cuda_status(cudaFuncSetAttribute(k_diag, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)SM::bytes),
-                         "staged smem attribute");
-        if (rc) return rc;
-        attr_done = true;
-    }
-    auto *k = checksum ? k_diag : k_fast;
-    k<<<(unsigned)tiles, T0 * T1, SM::bytes, stream>>>(
-        P, map, ptab, pff, ctab, nt0, reinterpret_cast<double2 *>(out), nvalid, checksum, ctr,
-        status);
+    auto *k = checksum ? focus_mixed_staged_kernel<CHUNK, T0, T1, W, true>
+                       : focus_mixed_staged_kernel<CHUNK, T0, T1, W, false>;
+    k<<<(unsigned)tiles, T0 * T1, SM::bytes, stream>>>(P, map, tb, nt0, o, ctr, status);
     return cuda_status(cudaGetLastError(), "focus_mixed_staged launch");
 }
+
+// (chunk, tile0, tile1, window) variants the staged kernels are built for.
+#define SARBP_STAGED_TILINGS(X) \
+    X(32, 16, 16, 128) X(32, 16, 16, 160) X(32, 16, 8, 128) X(32, 32, 8, 128) X(32, 64, 4, 128)
 
 int launch_staged(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L, char *ws,
                   double *out, int32_t *nvalid, uint64_t *checksum, uint64_t *counters,
                   cudaStream_t stream)
 {
-    const int key = T.chunk * 1000000 + T.tile0 * 1000 + T.tile1;
-    switch (key) {
-        case 32 * 1000000 + 32 * 1000 + 8:
-            return launch_staged_t<32, 32, 8, 128>(P, L, ws, out, nvalid, checksum, counters,
-                                                   stream);
-        case 32 * 1000000 + 64 * 1000 + 4:
-            return launch_staged_t<32, 64, 4, 128>(P, L, ws, out, nvalid, checksum, counters,
-                                                   stream);
-        case 32 * 1000000 + 16 * 1000 + 16:
-            return launch_staged_t<32, 16, 16, 128>(P, L, ws, out, nvalid, checksum, counters,
-                                                    stream);
-        default:
-            set_error("staged path: unsupported tuning chunk=%d tile=%dx%d (chunk 32 only)",
-                      T.chunk, T.tile0, T.tile1);
-            return SARBP_EINVAL;
+#define X(C, A, B, W)                                                                       \
+    if (T.chunk == C && T.tile0 == A && T.tile1 == B && T.window == W)                      \
+        return launch_staged_t<C, A, B, W>(P, L, ws, out, nvalid, checksum, counters, stream);
+    SARBP_STAGED_TILINGS(X)
+#undef X
+    set_error("staged path: unsupported tuning chunk=%d tile=%dx%d window=%d", T.chunk, T.tile0,
+              T.tile1, T.window);
+    return SARBP_EINVAL;
+}
+
+// ---------------------------------------------------------------------------
+// batches: many scenes, one persistent launch
+
+struct BatchHeader {
+    StatusBlock status;
+    unsigned long long cursor;      // next work item
+    int32_t nscenes, key;           // scene slots, tiling key of the batch
+    int64_t max_items;
+    unsigned char pad[256 - 8 - 8 - 8];
+};
+
+struct BatchLayout {
+    size_t header, scenes, items, total;
+};
+
+static BatchLayout batch_layout(int nscenes, int64_t max_items)
+{
+    BatchLayout L{};
+    L.header = 0;
+    L.scenes = (sizeof(BatchHeader) + 255) & ~(size_t)255;
+    L.items = (L.scenes + sizeof(BatchScene) * (size_t)nscenes + 255) & ~(size_t)255;
+    L.total = (L.items + sizeof(int2) * (size_t)max_items + 255) & ~(size_t)255;
+    return L;
+}
+
+int64_t batch_workspace_size(int nscenes, int64_t max_items)
+{
+    return (int64_t)batch_layout(nscenes, max_items).total;
+}
+
+static int tiling_tiles(const SceneParams &P, const sarbp_tuning &T, int64_t *nt0, int64_t *nt)
+{
+    if (T.tile0 <= 0 || T.tile1 <= 0) {
+        set_error("tiling: tile extents must be positive");
+        return SARBP_EINVAL;
     }
+    *nt0 = (P.dim0 + T.tile0 - 1) / T.tile0;
+    *nt = *nt0 * ((P.dim1 + T.tile1 - 1) / T.tile1);
+    return SARBP_OK;
+}
+
+int batch_set_scene(void *bws, size_t bytes, int slot, int nscenes, const SceneParams &P,
+                    const sarbp_tuning &T, void *scene_ws, size_t scene_ws_bytes, double *out,
+                    int32_t *nvalid, uint64_t *checksum, cudaStream_t stream)
+{
+    if (!T.staged || T.chunk != 32) {
+        set_error("batch path: needs the staged kernel with 32-pulse chunks");
+        return SARBP_EINVAL;
+    }
+    const BatchLayout BL = batch_layout(nscenes, 0);
+    if (!bws || slot < 0 || slot >= nscenes || bytes < BL.items) {
+        set_error("batch path: slot %d outside the %d-scene workspace", slot, nscenes);
+        return SARBP_EINVAL;
+    }
+    const MixedLayout L = mixed_layout(P.naz, T.chunk);
+    if (!scene_ws || scene_ws_bytes < L.total || !out) {
+        set_error("batch path: scene workspace (%zu < %zu bytes) or output missing",
+                  scene_ws_bytes, L.total);
+        return SARBP_EWORKSPACE;
+    }
+    BatchScene B;
+    memset(&B, 0, sizeof(B));
+    int rc = make_raw_map(P, T.window, T.chunk, &B.map);
+    if (rc) return rc;
+    B.P = P;
+    B.tables = tables_of(static_cast<char *>(scene_ws), L);
+    B.outputs = TileOutputs{reinterpret_cast<double2 *>(out), nvalid, checksum};
+    rc = tiling_tiles(P, T, &B.ntile0, &B.ntiles);
+    if (rc) return rc;
+    char *dst = static_cast<char *>(bws) + BL.scenes + sizeof(BatchScene) * (size_t)slot;
+    return cuda_status(cudaMemcpyAsync(dst, &B, sizeof(B), cudaMemcpyHostToDevice, stream),
+                       "batch scene upload");
+}
+
+int batch_set_items(void *bws, size_t bytes, int nscenes, const int32_t *items, int64_t n,
+                    cudaStream_t stream)
+{
+    const BatchLayout BL = batch_layout(nscenes, n);
+    if (!bws || bytes < BL.total || (n > 0 && !items)) {
+        set_error("batch path: workspace of %zu bytes too small for %lld items", bytes,
+                  (long long)n);
+        return SARBP_EWORKSPACE;
+    }
+    if (n == 0) return SARBP_OK;
+    return cuda_status(cudaMemcpyAsync(static_cast<char *>(bws) + BL.items, items,
+                                       sizeof(int2) * (size_t)n, cudaMemcpyHostToDevice, stream),
+                       "batch items upload");
+}
+
+template <int C, int A, int B, int W>
+static int launch_batch_t(char *bws, const BatchLayout &BL, int64_t n_items, bool diag,
+                          uint64_t *counters, cudaStream_t stream)
+{
+    using SM = StagedSmem<C, W>;
+    int rc = ensure_smem_attr<C, A, B, W>();
+    if (rc) return rc;
+    auto *k = diag ? focus_batch_staged_kernel<C, A, B, W, true>
+                   : focus_batch_staged_kernel<C, A, B, W, false>;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, A * B, SM::bytes),
+                     "batch occupancy");
+    if (rc) return rc;
+    const int64_t grid = std::min<int64_t>(n_items, (int64_t)std::max(1, per_sm) * sms);
+    auto *hdr = reinterpret_cast<BatchHeader *>(bws);
+    rc = cuda_status(cudaMemsetAsync(&hdr->cursor, 0, sizeof(hdr->cursor), stream),
+                     "batch cursor reset");
+    if (rc) return rc;
+    k<<<(unsigned)grid, A * B, SM::bytes, stream>>>(
+        reinterpret_cast<const BatchScene *>(bws + BL.scenes),
+        reinterpret_cast<const int2 *>(bws + BL.items), n_items, &hdr->cursor,
+        reinterpret_cast<unsigned long long *>(counters), &hdr->status);
+    return cuda_status(cudaGetLastError(), "focus_batch_staged launch");
+}
+
+int batch_focus(void *bws, size_t bytes, int nscenes, const sarbp_tuning &T, int64_t n_items,
+                bool diag, uint64_t *counters, cudaStream_t stream)
+{
+    const BatchLayout BL = batch_layout(nscenes, n_items);
+    if (!bws || bytes < BL.total) {
+        set_error("batch path: workspace of %zu bytes too small (%zu)", bytes, BL.total);
+        return SARBP_EWORKSPACE;
+    }
+    if (n_items <= 0) return SARBP_OK;
+    char *ws = static_cast<char *>(bws);
+#define X(C, A, B, W)                                                                       \
+    if (T.staged && T.chunk == C && T.tile0 == A && T.tile1 == B && T.window == W)          \
+        return launch_batch_t<C, A, B, W>(ws, BL, n_items, diag, counters, stream);
+    SARBP_STAGED_TILINGS(X)
+#undef X
+    set_error("batch path: unsupported tuning chunk=%d tile=%dx%d staged=%d", T.chunk, T.tile0,
+              T.tile1, T.staged);
+    return SARBP_EINVAL;
+}
+
+// Estimated cost of each tile of a scene: the sum of its pixels' kept
+// aperture lengths (nominal pixel-pulses), for ordering batch work.
+template <int T0, int T1>
+__global__ void tile_cost_kernel(const SceneParams P, int64_t ntile0, int64_t ntiles,
+                                 int64_t *__restrict__ costs)
+{
+    const int64_t tile = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tile >= ntiles) return;
+    const int64_t t0 = tile % ntile0, t1 = tile / ntile0;
+    int64_t c = 0;
+    for (int b = 0; b < T1; ++b)
+        for (int a = 0; a < T0; ++a) {
+            const int64_t i0 = t0 * T0 + a, i1 = t1 * T1 + b;
+            if (i0 >= P.dim0 || i1 >= P.dim1) continue;
+            const int64_t ii = i0 + P.dim0 * i1;
+            int64_t lo, hi;
+            if (pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi))
+                c += hi - lo + 1;
+        }
+    costs[tile] = c;
+}
+
+int tile_costs(const SceneParams &P, const sarbp_tuning &T, int64_t *costs, cudaStream_t stream)
+{
+    int64_t nt0, nt;
+    int rc = tiling_tiles(P, T, &nt0, &nt);
+    if (rc) return rc;
+    const unsigned blocks = (unsigned)((nt + 127) / 128);
+#define X(A, B)                                                                             \
+    if (T.tile0 == A && T.tile1 == B) {                                                     \
+        tile_cost_kernel<A, B><<<blocks, 128, 0, stream>>>(P, nt0, nt, costs);              \
+        return cuda_status(cudaGetLastError(), "tile_cost launch");                         \
+    }
+    X(16, 16) X(16, 8) X(32, 8) X(64, 4)
+#undef X
+    set_error("tile costs: unsupported tile %dx%d", T.tile0, T.tile1);
+    return SARBP_EINVAL;
+}
+
+int tile_count(const SceneParams &P, const sarbp_tuning &T, int64_t *nt)
+{
+    int64_t nt0;
+    return tiling_tiles(P, T, &nt0, nt);
 }
 
 }  // namespace sarbp

@@ -124,4 +124,16 @@ int launch_mixed_prepare(const SceneParams &P, const sarbp_tuning &T, void *work
 int launch_mixed_main(const SceneParams &P, const sarbp_tuning &T, void *workspace,
                       size_t ws_bytes, double *out, int32_t *nvalid, uint64_t *checksum,
                       uint64_t *counters, cudaStream_t stream);
+
+// batches of scenes in one persistent launch (focus_staged.cu)
+int64_t batch_workspace_size(int nscenes, int64_t max_items);
+int batch_set_scene(void *bws, size_t bytes, int slot, int nscenes, const SceneParams &P,
+                    const sarbp_tuning &T, void *scene_ws, size_t scene_ws_bytes, double *out,
+                    int32_t *nvalid, uint64_t *checksum, cudaStream_t stream);
+int batch_set_items(void *bws, size_t bytes, int nscenes, const int32_t *items, int64_t n,
+                    cudaStream_t stream);
+int batch_focus(void *bws, size_t bytes, int nscenes, const sarbp_tuning &T, int64_t n_items,
+                bool diag, uint64_t *counters, cudaStream_t stream);
+int tile_costs(const SceneParams &P, const sarbp_tuning &T, int64_t *costs, cudaStream_t stream);
+int tile_count(const SceneParams &P, const sarbp_tuning &T, int64_t *nt);
 }  // namespace sarbp
