@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tuning", type=str, default="",
-                    help="chunk,tile0,tile1[,staged] of the mixed kernel")
+                    help="chunk,tile0,tile1[,staged[,window]] of the mixed kernel")
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--workload", choices=["full", "profile"], default="full",
                     help="profile: the same geometry at 1000x250 pixels / 10001 pulses "
@@ -289,7 +289,7 @@ def run_ours(args, dist: Dist):
     tuning = resolve_tuning(None)
     if args.tuning:
         vals = [int(v) for v in args.tuning.split(",")]
-        for k, v in zip(("chunk", "tile0", "tile1", "staged"), vals):
+        for k, v in zip(("chunk", "tile0", "tile1", "staged", "window"), vals):
             setattr(tuning, k, v)
 
     spec, workload_name = workload_spec(args, dist.rank)

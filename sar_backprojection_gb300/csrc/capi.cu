@@ -96,20 +96,22 @@ bool build_params(const sarbp_scene *s, SceneParams *p)
     return true;
 }
 
-// Library default: the TMA-staged kernel, 32-pulse chunks, 16 x 16 pixel
-// tiles (fastest measured on the 4000 x 250 / 40001-pulse workload).
+// Library default: the TMA-staged kernel, 32-pulse chunks, 16 x 8 pixel tiles
+// with a 128-bin window (fastest measured on the 4000 x 250 / 40001-pulse
+// workload: the tile's range windows fit the staged box, so no pulse falls
+// back to L2).
 bool valid_tuning(sarbp_tuning *t)
 {
     if (t->chunk == 0 && t->tile0 == 0 && t->tile1 == 0 && t->staged == 0) {
         t->chunk = 32;
         t->tile0 = 16;
-        t->tile1 = 16;
+        t->tile1 = 8;
         t->staged = 1;
     }
     if (t->chunk == 0) t->chunk = 32;
     if (t->tile0 == 0 && t->tile1 == 0) {
         t->tile0 = 16;
-        t->tile1 = 16;
+        t->tile1 = 8;
     }
     if (t->staged && t->window == 0) t->window = 128;
     if (t->chunk != 32 && t->chunk != 64) {

@@ -50,7 +50,12 @@ __global__ void chunk_table_kernel(const SceneParams P, int chunk, float4 *__res
     float mx = 0.f, my = 0.f, mz = 0.f, m2 = 0.f;
     for (int j = lane; j < chunk; j += 32) {
         const int64_t k = c * chunk + j;
-        if (k >= P.naz) break;
+        if (k >= P.naz) {
+            // padding past the last pulse: copied with whole chunks by the
+            // staged kernel, must hold finite values (never a kept pulse)
+            ptab[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            continue;
+        }
         const double tx = P.tx[k], ty = P.ty[k], tz = P.tz[k];
         const double ex = tx - x0, ey = ty - y0, ez = tz - z0;
         const double e2 = ex * ex + ey * ey + ez * ez;

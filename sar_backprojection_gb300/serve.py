@@ -1,0 +1,318 @@
+"""Continuous-batching focusing service on one GPU.
+
+Requests (focusing jobs of different sizes) arrive over time.  The engine
+
+* admits a waiting job as soon as a scene slot and enough of the HBM budget
+  are free, uploading its inputs on a copy stream while other jobs' work runs
+  (the job's raw data and trajectory then stay resident until it finishes);
+* runs the device in *waves*: each wave is one launch of the persistent
+  batch kernel whose work queue holds pixel tiles of every admitted job, so a
+  job that arrives while others are on the GPU joins the next wave and its
+  tiles run alongside theirs; waves alternate between two streams and two
+  batch workspaces, so the next wave is already on the device and its CTAs
+  fill the tail of the running one;
+* reads a job's image back (pinned host memory) when its last tile is done,
+  then frees its slot and memory.
+
+Latency = completion of the image's device-to-host copy minus arrival time.
+Per-tile work is the same code as the single-scene kernel, so a job's image
+is bit-identical whether it ran alone or in the mix.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from .batch import staged_tuning
+from .focuser import resolve_tuning
+from .scene import DeviceScene, scene_to_device
+
+GB = 1 << 30
+
+
+def job_bytes(dim0: int, dim1: int, nra: int, naz: int) -> int:
+    """Device bytes a job holds while resident (inputs, image, workspace)."""
+    npix = dim0 * dim1
+    pitch = nra + (nra & 1)
+    return (8 * pitch * naz + 37 * npix + 24 * naz + 16 * npix + 56 * naz + 4096)
+
+
+@dataclass
+class Job:
+    """One focusing request: the reference's 13 positional arguments."""
+
+    job_id: int
+    args: tuple
+    arrival: float = 0.0                  # seconds after the start of the run
+    admitted: float | None = None
+    finished: float | None = None
+    image: np.ndarray | None = None
+    nominal: int = 0
+
+    @property
+    def shape(self):
+        return tuple(self.args[0].shape)
+
+    def nbytes(self) -> int:
+        raw = self.args[8]
+        return job_bytes(self.shape[0], self.shape[1], int(raw.shape[0]), int(raw.shape[1]))
+
+    @property
+    def latency(self) -> float | None:
+        return None if self.finished is None else self.finished - self.arrival
+
+
+@dataclass
+class _Active:
+    job: Job
+    slot: int
+    scene: DeviceScene
+    ws: torch.Tensor
+    out: torch.Tensor
+    host: torch.Tensor
+    tiles: deque                          # tile indices not yet launched, in cost order
+    in_flight: int = 0
+    done_event: torch.cuda.Event | None = None
+
+
+@dataclass
+class ServingReport:
+    jobs: list
+    wall_s: float
+    waves: int
+    gpu_launches: int
+    peak_bytes: int
+    latencies_ms: list = field(default_factory=list)
+
+    def summary(self) -> dict:
+        lat = np.array([j.latency for j in self.jobs if j.latency is not None]) * 1e3
+        work = sum(j.nominal for j in self.jobs)
+        return {"jobs": len(self.jobs), "completed": int(lat.size),
+                "p50_ms": float(np.percentile(lat, 50)) if lat.size else None,
+                "p99_ms": float(np.percentile(lat, 99)) if lat.size else None,
+                "mean_ms": float(lat.mean()) if lat.size else None,
+                "wall_s": self.wall_s, "pixel_pulses": work,
+                "gpix_pulse_per_s": work / self.wall_s / 1e9 if self.wall_s > 0 else None,
+                "waves": self.waves, "gpu_launches": self.gpu_launches,
+                "peak_resident_gb": self.peak_bytes / GB}
+
+
+class ServingEngine:
+    """Continuous batching of focusing jobs on one device (see module doc)."""
+
+    def __init__(self, device=None, budget_bytes: int = 150 * GB, max_slots: int = 32,
+                 wave_items: int | None = None, tuning=None, policy: str = "fifo"):
+        self.device = torch.device(device or "cuda")
+        self.lib = _lib.load()
+        self.tuning = staged_tuning() if tuning is None else resolve_tuning(tuning)
+        self.budget = int(budget_bytes)
+        self.max_slots = int(max_slots)
+        props = torch.cuda.get_device_properties(self.device)
+        self.wave_items = int(wave_items or 3 * 2 * props.multi_processor_count)
+        if policy not in ("fifo", "srpt"):
+            raise ValueError("policy must be 'fifo' or 'srpt'")
+        self.policy = policy
+        self.compute = [torch.cuda.Stream(self.device), torch.cuda.Stream(self.device)]
+        self.copy = torch.cuda.Stream(self.device)
+        nb = _lib.check(int(self.lib.sarbp_batch_workspace_size(self.max_slots,
+                                                                self.wave_items)))
+        self.bws_bytes = nb
+        self.bws = [torch.empty(nb, dtype=torch.uint8, device=self.device) for _ in range(2)]
+        self.free_slots = list(range(self.max_slots))
+        self.used = 0
+        self.peak = 0
+
+    # -- per job -----------------------------------------------------------
+
+    def _admit(self, job: Job, now: float) -> _Active:
+        slot = self.free_slots.pop(0)
+        tb = C.byref(self.tuning)
+        with torch.cuda.stream(self.copy):
+            scene = scene_to_device(*job.args, device=self.device)
+            ws_bytes = _lib.check(int(self.lib.sarbp_mixed_workspace_size(
+                C.byref(scene.struct()), tb)))
+            ws = torch.empty(ws_bytes, dtype=torch.uint8, device=self.device)
+            out = torch.empty((scene.npix, 2), dtype=torch.float64, device=self.device)
+            sp = self.copy.cuda_stream
+            _lib.check(self.lib.sarbp_mixed_prepare(C.byref(scene.struct()), tb,
+                                                    ws.data_ptr(), ws_bytes, sp))
+            nt = _lib.check(int(self.lib.sarbp_tile_count(C.byref(scene.struct()), tb)))
+            for b in self.bws:
+                _lib.check(self.lib.sarbp_batch_set_scene(
+                    b.data_ptr(), self.bws_bytes, self.max_slots, slot, C.byref(scene.struct()),
+                    tb, ws.data_ptr(), ws_bytes, out.data_ptr(), None, None, sp))
+        ready = torch.cuda.Event()
+        ready.record(self.copy)
+        for st in self.compute:
+            st.wait_event(ready)
+        job.admitted = now
+        job.nominal = _nominal(job.args)
+        host = torch.empty((scene.npix, 2), dtype=torch.float64, pin_memory=True)
+        self.used += job.nbytes()
+        self.peak = max(self.peak, self.used)
+        return _Active(job=job, slot=slot, scene=scene, ws=ws, out=out, host=host,
+                       tiles=deque(range(nt)))
+
+    def _retire(self, a: _Active, now: float):
+        j = a.job
+        flat = a.host.numpy().view(np.complex128).reshape(-1)
+        j.image = np.reshape(flat, (a.scene.dim0, a.scene.dim1), order="F")
+        j.finished = now
+        self.used -= j.nbytes()
+        self.free_slots.append(a.slot)
+
+    # -- waves -------------------------------------------------------------
+
+    def _build_wave(self, active: list[_Active]) -> list[tuple[_Active, int]]:
+        cand = [a for a in active if a.tiles]
+        if self.policy == "srpt":
+            cand.sort(key=lambda a: len(a.tiles))
+        else:
+            cand.sort(key=lambda a: a.job.arrival)
+        wave = []
+        for a in cand:
+            while a.tiles and len(wave) < self.wave_items:
+                wave.append((a, a.tiles.popleft()))
+            if len(wave) >= self.wave_items:
+                break
+        return wave
+
+    def _launch_wave(self, wave, turn: int) -> torch.cuda.Event:
+        items = np.array([[a.slot, t] for a, t in wave], dtype=np.int32)
+        for a, _ in wave:
+            a.in_flight += 1
+        stream, bws = self.compute[turn], self.bws[turn]
+        with torch.cuda.stream(stream):
+            sp = stream.cuda_stream
+            _lib.check(self.lib.sarbp_batch_set_items(bws.data_ptr(), self.bws_bytes,
+                                                      self.max_slots,
+                                                      items.ctypes.data_as(C.c_void_p),
+                                                      len(wave), sp))
+            _lib.check(self.lib.sarbp_batch_focus(bws.data_ptr(), self.bws_bytes,
+                                                  self.max_slots, C.byref(self.tuning),
+                                                  len(wave), 0, None, sp))
+        ev = torch.cuda.Event()
+        ev.record(stream)
+        return ev
+
+    # -- the loop ----------------------------------------------------------
+
+    def run(self, jobs: list[Job], clock=time.perf_counter, idle_sleep: float = 5e-5,
+            timeout_s: float = 600.0) -> ServingReport:
+        arrivals = sorted(jobs, key=lambda j: j.arrival)
+        pending: deque = deque()
+        active: list[_Active] = []
+        readbacks: list = []             # (event, active)
+        waves_in_flight: deque = deque()  # (event, wave, ws index)
+        nxt = 0
+        nwaves = 0
+        launches = 0
+        ws_turn = 0
+        t0 = clock()
+        while True:
+            now = clock() - t0
+            if now > timeout_s:
+                raise TimeoutError(f"serving run exceeded {timeout_s} s")
+            while nxt < len(arrivals) and arrivals[nxt].arrival <= now:
+                pending.append(arrivals[nxt])
+                nxt += 1
+            # admission: FIFO, by slots and HBM budget
+            while pending and self.free_slots and self.used + pending[0].nbytes() <= self.budget:
+                active.append(self._admit(pending.popleft(), now))
+                launches += 1            # chunk tables (uploads are copies)
+            if pending and not active and not self.free_slots:
+                raise RuntimeError("no scene slot free and nothing running")
+            if pending and not active and self.used + pending[0].nbytes() > self.budget:
+                raise RuntimeError(f"job {pending[0].job_id} needs more than the HBM budget")
+            # completed waves
+            while waves_in_flight and waves_in_flight[0][0].query():
+                _, wave, _ = waves_in_flight.popleft()
+                for a, _t in wave:
+                    a.in_flight -= 1
+                for a in {id(a): a for a, _ in wave}.values():
+                    if not a.tiles and a.in_flight == 0 and a.done_event is None:
+                        # every wave with this job's tiles has completed: read back
+                        with torch.cuda.stream(self.copy):
+                            a.host.copy_(a.out, non_blocking=True)
+                            ev = torch.cuda.Event()
+                            ev.record(self.copy)
+                        a.done_event = ev
+                        readbacks.append(a)
+            # keep two waves queued on the device
+            while len(waves_in_flight) < 2:
+                wave = self._build_wave(active)
+                if not wave:
+                    break
+                turn = ws_turn
+                ws_turn ^= 1
+                ev = self._launch_wave(wave, turn)
+                waves_in_flight.append((ev, wave, turn))
+                nwaves += 1
+                launches += 1
+            # finished read-backs
+            still = []
+            for a in readbacks:
+                if a.done_event.query():
+                    self._retire(a, clock() - t0)
+                    active.remove(a)
+                else:
+                    still.append(a)
+            readbacks = still
+            if nxt >= len(arrivals) and not pending and not active:
+                break
+            if idle_sleep:
+                time.sleep(idle_sleep)
+        torch.cuda.synchronize(self.device)
+        return ServingReport(jobs=jobs, wall_s=clock() - t0, waves=nwaves,
+                             gpu_launches=launches, peak_bytes=self.peak)
+
+
+def _nominal(args) -> int:
+    """Nominal pixel-pulses of a job from its host Mask and Sint arguments."""
+    m = np.asarray(args[3]).astype(np.uint8).reshape(-1)
+    s = np.asarray(args[12]).astype(np.int64).reshape(-1)
+    jj = np.where(s >= 0, (s + 1) // 2, -((-s) // 2)) * 2 + 1
+    return int(np.where((m == 1) & (s != -9999) & (jj > 0), jj, 0).sum())
+
+
+def poisson_arrivals(n: int, rate_per_s: float, seed: int = 0) -> np.ndarray:
+    """Arrival times (s) of a Poisson process with the given rate."""
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate_per_s, n))
+
+
+def run_fp64_sequential(jobs: list[Job], device=None) -> dict:
+    """Plain FP64 kernel, one job at a time in arrival order (the comparator).
+
+    Each job is uploaded, focused and read back before the next starts; the
+    service time of job k starts when both it has arrived and job k-1 is done.
+    """
+    from .focuser import focus
+    dev = torch.device(device or "cuda")
+    clock_free = 0.0
+    lat = []
+    work = 0
+    busy = 0.0
+    for j in sorted(jobs, key=lambda j: j.arrival):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        sc = scene_to_device(*j.args, device=dev)
+        res = focus(sc, "fp64")
+        res.image.cpu()
+        torch.cuda.synchronize(dev)
+        svc = time.perf_counter() - t0
+        start = max(j.arrival, clock_free)
+        clock_free = start + svc
+        lat.append(clock_free - j.arrival)
+        work += sc.nominal_pixel_pulses()
+        busy += svc
+        del sc, res
+    lat = np.array(lat) * 1e3
+    return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "busy_s": busy, "pixel_pulses": work, "gpix_pulse_per_s": work / busy / 1e9}

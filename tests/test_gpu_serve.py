@@ -1,0 +1,73 @@
+"""Serving: jobs that overlap on the device give the same image as alone.
+
+A Poisson stream of small focusing jobs of different sizes runs through the
+continuous-batching engine (jobs admitted while others run, their tiles mixed
+in the same persistent launches).  Each job's image must be bit-identical to
+the single-scene staged kernel's image of the same inputs, and the HBM budget
+must hold.
+"""
+import numpy as np
+import pytest
+import torch
+
+from sar_backprojection_gb300 import batch, focus, scene_to_device, serve, synth
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(128, 32, 2001, 200, 260), (256, 48, 3001, 400, 600), (96, 40, 2401, 900, 1300),
+         (160, 64, 4001, 1200, 1600), (64, 32, 2001, 300, 400), (192, 32, 3001, 600, 800)]
+
+
+@pytest.fixture(scope="module")
+def jobs():
+    out = []
+    arrivals = serve.poisson_arrivals(len(SIZES) * 2, rate_per_s=400.0, seed=3)
+    for i in range(len(SIZES) * 2):
+        d0, d1, naz, s_lo, s_hi = SIZES[i % len(SIZES)]
+        spec = synth.scaled_full(200 + i, d0, d1, naz, s_lo, s_hi)
+        sc = synth.generate(spec)                      # host (NumPy) inputs
+        out.append(serve.Job(job_id=i, args=synth.focus_args(sc), arrival=float(arrivals[i])))
+    return out
+
+
+def _alone(job, tuning):
+    ds = scene_to_device(*job.args, device="cuda")
+    res = focus(ds, "mixed", tuning=tuning)
+    torch.cuda.synchronize()
+    return res.to_numpy(ds.dim0, ds.dim1)
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.uint64)
+
+
+def test_each_job_same_alone_and_in_the_mix(jobs):
+    tuning = batch.staged_tuning()
+    eng = serve.ServingEngine(budget_bytes=8 * serve.GB, max_slots=8, wave_items=96,
+                              tuning=tuning)
+    rep = eng.run(jobs)
+    s = rep.summary()
+    assert s["completed"] == len(jobs)
+    assert s["p99_ms"] >= s["p50_ms"] > 0
+    assert rep.peak_bytes <= 8 * serve.GB
+    assert rep.waves >= 2
+    for j in jobs:
+        assert j.image is not None and j.image.shape == j.shape
+        assert np.array_equal(_bits(j.image), _bits(_alone(j, tuning))), f"job {j.job_id}"
+
+
+def test_budget_limits_residency(jobs):
+    small = jobs[:4]
+    for j in small:
+        j.admitted = j.finished = None
+        j.image = None
+    budget = max(j.nbytes() for j in small) + 1     # one job resident at a time
+    eng = serve.ServingEngine(budget_bytes=budget, max_slots=4, wave_items=64)
+    rep = eng.run(small)
+    assert rep.summary()["completed"] == len(small)
+    assert rep.peak_bytes <= budget
+
+
+def test_fp64_sequential_comparator(jobs):
+    r = serve.run_fp64_sequential(jobs[:3])
+    assert r["p99_ms"] >= r["p50_ms"] > 0 and r["pixel_pulses"] > 0
