@@ -57,6 +57,13 @@ def parse():
     ap.add_argument("--tuning", type=str, default="",
                     help="chunk,tile0,tile1[,staged[,window]] of the mixed kernel")
     ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--batch-scenes", type=int, default=48,
+                    help="uneven scenes focused in one persistent graph-captured launch "
+                         "(0: skip the batched measurement)")
+    ap.add_argument("--serve-jobs", type=int, default=500,
+                    help="Poisson-arrival focusing jobs per arrival rate (0: skip serving)")
+    ap.add_argument("--serve-rates", type=str, default="0.25,0.5,0.9",
+                    help="arrival rates as fractions of the measured job capacity")
     ap.add_argument("--workload", choices=["full", "profile"], default="full",
                     help="profile: the same geometry at 1000x250 pixels / 10001 pulses "
                          "(381 MB of raw data), a small case for ncu captures")
@@ -271,6 +278,100 @@ def run_reference(args, dist: Dist):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args, dev, tuning_default):
+    """Uneven scenes: mixed precision in one persistent graph-captured launch
+    (autotuned tiling) vs the plain FP64 kernel one scene at a time."""
+    import torch
+
+    from sar_backprojection_gb300 import batch, focus, quality, scene_to_device, synth
+
+    specs = synth.uneven_specs(args.batch_scenes)
+    scenes = [scene_to_device(*synth.focus_args(synth.generate(sp, raw_device=str(dev))),
+                              device=dev) for sp in specs]
+    work = sum(sc.nominal_pixel_pulses() for sc in scenes)
+    at = batch.Autotuner(repeats=2)
+    tuning = at.pick(scenes)
+    bf = batch.BatchFocuser(scenes, tuning, graph=True)
+    for _ in range(3):
+        bf.run()
+    steps = max(5, args.steps // 5)
+    ms = batch.time_steps(bf.run, steps, dev)
+    # FP64, one scene at a time
+    f_ms = 0.0
+    coh, rms = 1.0, 0.0
+    imgs = bf.images()
+    for sc, img in zip(scenes, imgs):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        r = focus(sc, "fp64")
+        b.record()
+        torch.cuda.synchronize(dev)
+        f_ms += a.elapsed_time(b)
+        q = quality.compare(torch.view_as_real(img.t().reshape(-1)).cpu().numpy(),
+                            r.image.cpu().numpy())
+        coh = min(coh, q["coherence"])
+        rms = max(rms, q["rms_phase_mrad"])
+    res = {
+        "scenes": len(scenes), "nominal_pixel_pulses": work,
+        "value": work / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms, "steps": steps,
+        "launch": "one CUDA graph per step: per-scene chunk tables + one persistent kernel",
+        "tuning": tuning.as_dict(), "autotune_ms": next(iter(at.timings.values())),
+        "fp64_one_at_a_time": {"value": work / (f_ms * 1e-3) / 1e9, "ms": f_ms},
+        "speedup_vs_fp64": f_ms / ms,
+        "worst_scene": {"coherence": coh, "rms_phase_mrad": rms},
+        "gpu_launches_per_step": bf.launches_per_step(),
+    }
+    del bf, scenes
+    torch.cuda.empty_cache()
+    return res
+
+
+def run_serving(args, dev):
+    """Poisson stream of focusing jobs (sizes of the uneven-scene mix) through
+    the continuous-batching engine at swept arrival rates, vs plain FP64 one
+    job at a time."""
+    import numpy as np
+    import torch
+
+    from sar_backprojection_gb300 import serve, synth
+
+    pool_specs = synth.uneven_specs(16, seed=5)
+    pool = []
+    for sp in pool_specs:
+        sc = synth.generate(sp, raw_device=str(dev))
+        raw = torch.empty((sp.naz, sp.nra), dtype=torch.complex64, pin_memory=True)
+        raw.copy_(sc["RawData"].t())
+        args13 = list(synth.focus_args(sc))
+        args13[8] = raw.t()
+        pool.append(tuple(args13))
+    rng = np.random.default_rng(11)
+    picks = rng.integers(0, len(pool), args.serve_jobs)
+    # capacity: a saturating run (all jobs at t=0)
+    def make(arrivals):
+        return [serve.Job(job_id=i, args=pool[k], arrival=float(t))
+                for i, (k, t) in enumerate(zip(picks, arrivals))]
+    eng = serve.ServingEngine(device=dev, budget_bytes=150 * serve.GB, max_slots=32)
+    sat = eng.run(make(np.zeros(args.serve_jobs))).summary()
+    cap = sat["completed"] / sat["wall_s"]
+    sweep = []
+    for frac in (float(x) for x in args.serve_rates.split(",")):
+        rate = frac * cap
+        eng = serve.ServingEngine(device=dev, budget_bytes=150 * serve.GB, max_slots=32)
+        rep = eng.run(make(serve.poisson_arrivals(args.serve_jobs, rate, seed=7))).summary()
+        rep["rate_jobs_per_s"] = rate
+        rep["load"] = frac
+        sweep.append(rep)
+    n64 = min(args.serve_jobs, 100)
+    f64 = serve.run_fp64_sequential(make(serve.poisson_arrivals(n64, 0.5 * cap, seed=7)),
+                                    device=dev)
+    f64["jobs"] = n64
+    f64["rate_jobs_per_s"] = 0.5 * cap
+    return {"jobs_per_rate": args.serve_jobs, "budget_gb": 150, "capacity_jobs_per_s": cap,
+            "saturated": sat, "sweep": sweep, "fp64_one_job_at_a_time": f64,
+            "what": "latency = arrival to image in host memory; inputs uploaded from pinned "
+                    "host memory per job"}
+
+
 def run_ours(args, dist: Dist):
     import ctypes as C
 
@@ -425,6 +526,9 @@ def run_ours(args, dist: Dist):
                "p99_ms": 1e3 * float(np.percentile(ts, 99)),
                "what": "single-scene drop-in call latency (host inputs to host image)"}
 
+    batch_res = run_batch(args, dev, tuning) if args.batch_scenes > 0 else None
+    serving_res = run_serving(args, dev) if args.serve_jobs > 0 else None
+
     cpu = None
     if not args.no_cpu_baseline and dist.rank == 0:
         from oracle import oracle
@@ -458,7 +562,11 @@ def run_ours(args, dist: Dist):
                          "ambiguous_bins_rederived": counters[_lib.CTR_AMBIGUOUS]}
                         if q else {"ambiguous_bins_rederived": counters[_lib.CTR_AMBIGUOUS]}),
             "window_misses": counters[_lib.CTR_WINDOW_MISS],
-            "latency": lat,
+            "latency": (serving_res["sweep"][len(serving_res["sweep"]) // 2]
+                        if serving_res else lat),
+            "single_call_latency": lat,
+            "batch": batch_res,
+            "serving": serving_res,
             "roofline": {"bound": "fp32_sfu_issue", "achieved": achieved, "peak": peak,
                          "unit": UNIT, "frac": achieved / peak, "traffic": traffic,
                          "kernel_ms": kernel_ms,

@@ -30,7 +30,7 @@ from .scene import DeviceScene
 STAGED_TILINGS = ((16, 16, 128), (16, 16, 160), (16, 8, 128), (32, 8, 128), (64, 4, 128))
 
 
-def staged_tuning(tile0: int = 16, tile1: int = 8, window: int = 128) -> _lib.Tuning:
+def staged_tuning(tile0: int = 16, tile1: int = 16, window: int = 160) -> _lib.Tuning:
     return resolve_tuning({"chunk": 32, "tile0": tile0, "tile1": tile1, "staged": 1,
                            "window": window})
 

@@ -96,24 +96,24 @@ bool build_params(const sarbp_scene *s, SceneParams *p)
     return true;
 }
 
-// Library default: the TMA-staged kernel, 32-pulse chunks, 16 x 8 pixel tiles
-// with a 128-bin window (fastest measured on the 4000 x 250 / 40001-pulse
-// workload: the tile's range windows fit the staged box, so no pulse falls
-// back to L2).
+// Library default: the TMA-staged kernel, 32-pulse chunks, 16 x 16 pixel
+// tiles with a 160-bin window (fastest measured on the 4000 x 250 /
+// 40001-pulse workload).
 bool valid_tuning(sarbp_tuning *t)
 {
     if (t->chunk == 0 && t->tile0 == 0 && t->tile1 == 0 && t->staged == 0) {
         t->chunk = 32;
         t->tile0 = 16;
-        t->tile1 = 8;
+        t->tile1 = 16;
         t->staged = 1;
+        t->window = 160;
     }
     if (t->chunk == 0) t->chunk = 32;
     if (t->tile0 == 0 && t->tile1 == 0) {
         t->tile0 = 16;
-        t->tile1 = 8;
+        t->tile1 = 16;
     }
-    if (t->staged && t->window == 0) t->window = 128;
+    if (t->staged && t->window == 0) t->window = (t->tile0 * t->tile1 >= 256) ? 160 : 128;
     if (t->chunk != 32 && t->chunk != 64) {
         set_error("tuning.chunk must be 32 or 64 (got %d)", t->chunk);
         return false;

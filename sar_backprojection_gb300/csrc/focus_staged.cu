@@ -42,7 +42,7 @@ struct StagedSmem {
     static constexpr size_t raw_bytes = (size_t)CHUNK * W * sizeof(float2);
     static constexpr size_t tab_bytes = (size_t)CHUNK * sizeof(float4);
     static constexpr size_t stage_bytes = raw_bytes + tab_bytes;
-    static constexpr size_t bytes = 2 * stage_bytes + 1024;   // + alignment slack
+    static constexpr size_t bytes = 2 * stage_bytes + 128;    // + alignment slack
 };
 
 template <int T0, int T1>
@@ -278,7 +278,9 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                 const bool fast = __all_sync(0xffffffffu, !work || (jmin == 0 &&
                                                                     jmax == CHUNK - 1 &&
                                                                     win_ok && !exact));
-                if (exact) {
+                if (!__any_sync(0xffffffffu, work)) {
+                    // no pixel of this warp has pulses in the chunk
+                } else if (exact) {
                     const double px = P.x[ii], py = P.y[ii], pz = P.z[ii];
                     double sre = 0.0, sim = 0.0;
                     for (int j = jmin; j <= jmax; ++j) {
@@ -433,8 +435,9 @@ __device__ __forceinline__ StagedCta staged_cta_init(unsigned char *smem_dyn, ui
                                                      long long *s_hi)
 {
     StagedCta cta;
+    // TMA tile loads without swizzle need 128-byte aligned destinations
     cta.smem = reinterpret_cast<unsigned char *>(
-        (reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~(uintptr_t)1023);
+        (reinterpret_cast<uintptr_t>(smem_dyn) + 127) & ~(uintptr_t)127);
     cta.full_bar = full_bar;
     cta.s_wlo = s_wlo;
     cta.s_whi = s_whi;
