@@ -339,3 +339,17 @@ def input_digest(scene: dict) -> str:
         h.update(k.encode())
         h.update(np.ascontiguousarray(a.reshape(-1, order="F")).tobytes())
     return h.hexdigest()
+
+
+def azimuth_columns(scene: dict) -> dict:
+    """The same scene with azimuth along the DEM's second axis.
+
+    The large-scene files of the reference are (DimRg, DimAz) grids batched
+    by azimuth columns (main_gpu.py:321-324, :415-434); the generators here
+    put azimuth first.  Transposes the six DEM-grid arrays (column-major kept);
+    trajectory and raw data are unchanged.
+    """
+    out = dict(scene)
+    for k in ("xxg1", "yyg1", "zzg1", "Mask", "Index", "Sint"):
+        out[k] = np.asfortranarray(np.asarray(scene[k]).T)
+    return out
