@@ -84,12 +84,15 @@ def config_full(seed: int = 2) -> SceneSpec:
 
 def scaled_full(seed: int, dim0: int, dim1: int, naz: int, sint_lo: int, sint_hi: int,
                 name: str | None = None) -> SceneSpec:
-    """A ``config_full``-like scene at its own size (uneven batch / serving)."""
+    """A ``config_full``-like scene at its own size (uneven batch / serving).
+
+    The DEM spans the whole track in azimuth (dim0 pixels over naz pulses) and
+    keeps the 4 m ground-range spacing (a dim1 x 4 m swath)."""
     track = 0.5 * (naz - 1)
     az = track / dim0
     return replace(config_full(seed), name=name or f"scene_{dim0}x{dim1}_{naz}", dim0=dim0,
                    dim1=dim1, az_spacing=az, x0=0.5 * az, naz=naz, sint_lo=sint_lo,
-                   sint_hi=sint_hi, rg_spacing=4.0 * 250 / max(dim1, 1) if dim1 < 250 else 4.0,
+                   sint_hi=sint_hi, rg_spacing=4.0,
                    n_targets=max(8, int(200 * dim0 * dim1 / 1.0e6)))
 
 
