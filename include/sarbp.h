@@ -74,14 +74,19 @@ typedef struct sarbp_scene {
  * Tuning of the mixed-precision kernel.  An all-zero struct (or NULL) selects
  * the library default; sarbp_default_tuning() fills the defaults explicitly.
  * Supported: staged=0 with chunk 32/64 and tiles 32x8, 64x4, 16x16; staged=1
- * with chunk 32 and (tile, window) 16x16/128, 16x16/160, 16x8/128, 32x8/128,
- * 64x4/128.
+ * or 2 with chunk 32 and (tile, window) 16x16/128, 16x16/160, 16x8/128,
+ * 32x8/128, 64x4/128.  staged=2 runs the staged kernel on a persistent grid
+ * that drains a queue of the scene's tiles in decreasing estimated cost; the
+ * queue (built by sarbp_mixed_prepare) adds a few bytes per tile to the
+ * workspace.  Images are bit-identical across staged=1 and staged=2.
  */
 typedef struct sarbp_tuning {
     int32_t chunk;        /* pulses per chunk: 32 or 64                       */
     int32_t tile0;        /* pixel-tile extent along dim0 (power of two)      */
     int32_t tile1;        /* pixel-tile extent along dim1                     */
-    int32_t staged;       /* 1: TMA-staged shared-memory raw window, 0: L1/L2 gathers */
+    int32_t staged;       /* 0: L1/L2 gathers; 1: TMA-staged raw window, one CTA per
+                             tile; 2: staged, persistent grid over a cost-ordered
+                             tile queue */
     int32_t window;       /* staged: range bins staged per pulse chunk (0: default) */
     int32_t reserved[3];
 } sarbp_tuning;
@@ -150,7 +155,9 @@ SARBP_API int sarbp_focus_mixed(const sarbp_scene *scene,
  * The two halves of sarbp_focus_mixed, for callers that keep a scene
  * resident and focus it repeatedly (serving, benchmarking): _prepare builds
  * the per-pulse chunk tables in the workspace (they depend on the trajectory
- * only), _prepared runs the focusing kernel on a prepared workspace.
+ * only) and, for staged=2, the cost-ordered tile queue (it depends on the
+ * mask, sint and index arrays); _prepared runs the focusing kernel on a
+ * prepared workspace.
  * sarbp_focus_mixed == sarbp_mixed_prepare + sarbp_focus_mixed_prepared.
  * Same reference counterpart as sarbp_focus_fp64.
  */

@@ -68,6 +68,8 @@ class BatchFocuser:
         self.tuning = staged_tuning() if tuning is None else resolve_tuning(tuning)
         if not self.tuning.staged or self.tuning.chunk != 32:
             raise ValueError("the batch path runs the staged kernel (staged=1, chunk=32)")
+        # the batch has its own (scene, tile) queue: no per-scene tile queue
+        self.tuning.staged = 1
         self.diagnostics = diagnostics
         self.counters = (torch.zeros(_lib.NUM_COUNTERS, dtype=torch.int64, device=self.device)
                          if diagnostics else None)

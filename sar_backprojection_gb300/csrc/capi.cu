@@ -96,16 +96,16 @@ bool build_params(const sarbp_scene *s, SceneParams *p)
     return true;
 }
 
-// Library default: the TMA-staged kernel, 32-pulse chunks, 16 x 16 pixel
-// tiles with a 160-bin window (fastest measured on the 4000 x 250 /
-// 40001-pulse workload).
+// Library default: the TMA-staged kernel on a persistent grid over the
+// cost-ordered tile queue, 32-pulse chunks, 16 x 16 pixel tiles with a
+// 160-bin window (fastest measured on the 4000 x 250 / 40001-pulse workload).
 bool valid_tuning(sarbp_tuning *t)
 {
     if (t->chunk == 0 && t->tile0 == 0 && t->tile1 == 0 && t->staged == 0) {
         t->chunk = 32;
         t->tile0 = 16;
         t->tile1 = 16;
-        t->staged = 1;
+        t->staged = 2;
         t->window = 160;
     }
     if (t->chunk == 0) t->chunk = 32;
@@ -114,6 +114,10 @@ bool valid_tuning(sarbp_tuning *t)
         t->tile1 = 16;
     }
     if (t->staged && t->window == 0) t->window = (t->tile0 * t->tile1 >= 256) ? 160 : 128;
+    if (t->staged < 0 || t->staged > 2) {
+        set_error("tuning.staged must be 0, 1 or 2 (got %d)", t->staged);
+        return false;
+    }
     if (t->chunk != 32 && t->chunk != 64) {
         set_error("tuning.chunk must be 32 or 64 (got %d)", t->chunk);
         return false;
@@ -163,7 +167,7 @@ SARBP_API int64_t sarbp_mixed_workspace_size(const sarbp_scene *scene, const sar
     sarbp_tuning T{};
     if (tuning) T = *tuning;
     if (!valid_tuning(&T)) return SARBP_EINVAL;
-    return (int64_t)mixed_layout(P.naz, T.chunk).total;
+    return (int64_t)mixed_layout(P, T).total;
 }
 
 static int mixed_args(const sarbp_scene *scene, const sarbp_tuning *tuning, SceneParams *P,

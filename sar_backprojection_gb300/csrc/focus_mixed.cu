@@ -16,9 +16,11 @@ namespace sarbp {
 
 static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
-MixedLayout mixed_layout(int64_t naz, int chunk)
+MixedLayout mixed_layout(const SceneParams &P, const sarbp_tuning &T)
 {
     MixedLayout L{};
+    const int chunk = T.chunk;
+    const int64_t naz = P.naz;
     size_t off = align256(sizeof(StatusBlock));
     const int64_t nchunks = (naz + chunk - 1) / chunk;
     L.ptab = off;      // padded to whole chunks: the staged kernel copies whole chunks
@@ -27,6 +29,24 @@ MixedLayout mixed_layout(int64_t naz, int chunk)
     off = align256(off + sizeof(PulseFF) * (size_t)naz);
     L.ctab = off;
     off = align256(off + sizeof(ChunkRef) * (size_t)nchunks);
+    L.base = off;
+    if (T.staged == 2 && T.tile0 > 0 && T.tile1 > 0) {
+        const int64_t nt = ((P.dim0 + T.tile0 - 1) / T.tile0) * ((P.dim1 + T.tile1 - 1) / T.tile1);
+        L.ntiles = nt;
+        L.keys_in = off;
+        off = align256(off + 4 * (size_t)nt);
+        L.vals_in = off;
+        off = align256(off + 4 * (size_t)nt);
+        L.keys_out = off;
+        off = align256(off + 4 * (size_t)nt);
+        L.vals_out = off;
+        off = align256(off + 4 * (size_t)nt);
+        L.sort_tmp = off;
+        L.sort_tmp_bytes = tile_sort_bytes(nt);
+        off = align256(off + L.sort_tmp_bytes);
+        L.cursor = off;
+        off = align256(off + sizeof(unsigned long long));
+    }
     L.total = off;
     return L;
 }
@@ -273,8 +293,8 @@ static int launch_gather(const SceneParams &P, const MixedLayout &L, char *ws, d
 }
 
 int launch_staged(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L, char *ws,
-                  double *out, int32_t *nvalid, uint64_t *checksum, uint64_t *counters,
-                  cudaStream_t stream);
+                  bool queued, double *out, int32_t *nvalid, uint64_t *checksum,
+                  uint64_t *counters, cudaStream_t stream);
 
 int launch_chunk_table(const SceneParams &P, int chunk, char *ws, const MixedLayout &L,
                        cudaStream_t stream)
@@ -301,17 +321,22 @@ static int check_workspace(const MixedLayout &L, void *workspace, size_t ws_byte
 int launch_mixed_prepare(const SceneParams &P, const sarbp_tuning &T, void *workspace,
                          size_t ws_bytes, cudaStream_t stream)
 {
-    const MixedLayout L = mixed_layout(P.naz, T.chunk);
+    const MixedLayout L = mixed_layout(P, T);
     int rc = check_workspace(L, workspace, ws_bytes);
     if (rc) return rc;
-    return launch_chunk_table(P, T.chunk, static_cast<char *>(workspace), L, stream);
+    char *ws = static_cast<char *>(workspace);
+    rc = launch_chunk_table(P, T.chunk, ws, L, stream);
+    if (rc) return rc;
+    // persistent staged path: tiles in decreasing estimated cost
+    if (T.staged == 2) return tile_order(P, T, L, ws, stream);
+    return SARBP_OK;
 }
 
 int launch_mixed_main(const SceneParams &P, const sarbp_tuning &T, void *workspace,
                       size_t ws_bytes, double *out, int32_t *nvalid, uint64_t *checksum,
                       uint64_t *counters, cudaStream_t stream)
 {
-    const MixedLayout L = mixed_layout(P.naz, T.chunk);
+    const MixedLayout L = mixed_layout(P, T);
     int rc = check_workspace(L, workspace, ws_bytes);
     if (rc) return rc;
     if (P.pitch * (int64_t)T.chunk + P.nra >= (1LL << 31)) {
@@ -321,7 +346,7 @@ int launch_mixed_main(const SceneParams &P, const sarbp_tuning &T, void *workspa
     }
     char *ws = static_cast<char *>(workspace);
     if (T.staged)
-        return launch_staged(P, T, L, ws, out, nvalid, checksum, counters, stream);
+        return launch_staged(P, T, L, ws, T.staged == 2, out, nvalid, checksum, counters, stream);
     const int key = T.chunk * 1000000 + T.tile0 * 1000 + T.tile1;
     switch (key) {
         case 32 * 1000000 + 32 * 1000 + 8:

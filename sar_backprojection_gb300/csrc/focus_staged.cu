@@ -26,6 +26,7 @@
 #include <cstdio>
 #include <cstring>
 
+#include <cub/device/device_radix_sort.cuh>
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -507,6 +508,40 @@ focus_mixed_staged_kernel(const SceneParams P, const __grid_constant__ CUtensorM
     flush_stats(st, counters);
 }
 
+// One scene, persistent grid: CTAs pull tiles in decreasing estimated cost
+// (the order prepared in the workspace) until the queue is empty, so the
+// longest tiles start first and no wave of CTAs ends half empty.
+template <int CHUNK, int T0, int T1, int W, bool kChecksum>
+__global__ void __launch_bounds__(T0 *T1)
+focus_mixed_staged_queue_kernel(const SceneParams P, const __grid_constant__ CUtensorMap raw_map,
+                                const TileTables tb, int64_t ntile0,
+                                const int32_t *__restrict__ order, int64_t ntiles,
+                                unsigned long long *cursor, const TileOutputs o,
+                                unsigned long long *__restrict__ counters, StatusBlock *status)
+{
+    extern __shared__ unsigned char smem_dyn[];
+    __shared__ __align__(8) uint64_t full_bar[2];
+    __shared__ int s_wlo[kMaxPassChunks], s_whi[kMaxPassChunks];
+    __shared__ long long s_lo, s_hi;
+    __shared__ long long s_item[2];
+    StagedCta cta = staged_cta_init<CHUNK, W>(smem_dyn, full_bar, s_wlo, s_whi, &s_lo, &s_hi);
+    TileStats st{0, 0, 0};
+    for (int round = 0;; ++round) {
+        if (threadIdx.x == 0) s_item[round & 1] = (long long)atomicAdd(cursor, 1ull);
+        __syncthreads();
+        const long long item = s_item[round & 1];
+        if (item >= ntiles) break;
+        const int64_t tile = order[item];
+        const bool ok = staged_tile<CHUNK, T0, T1, W, kChecksum>(
+            cta, P, &raw_map, tb, tile % ntile0, tile / ntile0, o, st);
+        if (!ok) {
+            staged_abort(cta, status, counters);
+            return;
+        }
+    }
+    flush_stats(st, counters);
+}
+
 // Many scenes in one persistent launch: CTAs pull (scene, tile) work items
 // from a device queue (a list ordered by decreasing estimated cost and an
 // atomic cursor) until it is empty.
@@ -599,8 +634,10 @@ static int ensure_smem_attr()
     int rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
     if (rc) return rc;
     if (dev < 0 || dev >= 64 || done[dev]) return SARBP_OK;
-    const void *ks[4] = {(const void *)focus_mixed_staged_kernel<CHUNK, T0, T1, W, false>,
+    const void *ks[6] = {(const void *)focus_mixed_staged_kernel<CHUNK, T0, T1, W, false>,
                          (const void *)focus_mixed_staged_kernel<CHUNK, T0, T1, W, true>,
+                         (const void *)focus_mixed_staged_queue_kernel<CHUNK, T0, T1, W, false>,
+                         (const void *)focus_mixed_staged_queue_kernel<CHUNK, T0, T1, W, true>,
                          (const void *)focus_batch_staged_kernel<CHUNK, T0, T1, W, false>,
                          (const void *)focus_batch_staged_kernel<CHUNK, T0, T1, W, true>};
     for (const void *k : ks) {
@@ -623,8 +660,9 @@ static TileTables tables_of(char *ws, const MixedLayout &L)
 }
 
 template <int CHUNK, int T0, int T1, int W>
-int launch_staged_t(const SceneParams &P, const MixedLayout &L, char *ws, double *out,
-                    int32_t *nvalid, uint64_t *checksum, uint64_t *counters, cudaStream_t stream)
+int launch_staged_t(const SceneParams &P, const MixedLayout &L, char *ws, bool queued,
+                    double *out, int32_t *nvalid, uint64_t *checksum, uint64_t *counters,
+                    cudaStream_t stream)
 {
     using SM = StagedSmem<CHUNK, W>;
     const int64_t nt0 = (P.dim0 + T0 - 1) / T0, nt1 = (P.dim1 + T1 - 1) / T1;
@@ -642,10 +680,28 @@ int launch_staged_t(const SceneParams &P, const MixedLayout &L, char *ws, double
     const TileOutputs o{reinterpret_cast<double2 *>(out), nvalid, checksum};
     auto *status = reinterpret_cast<StatusBlock *>(ws + L.status);
     auto *ctr = reinterpret_cast<unsigned long long *>(counters);
-    auto *k = checksum ? focus_mixed_staged_kernel<CHUNK, T0, T1, W, true>
-                       : focus_mixed_staged_kernel<CHUNK, T0, T1, W, false>;
-    k<<<(unsigned)tiles, T0 * T1, SM::bytes, stream>>>(P, map, tb, nt0, o, ctr, status);
-    return cuda_status(cudaGetLastError(), "focus_mixed_staged launch");
+    if (!queued) {
+        auto *k = checksum ? focus_mixed_staged_kernel<CHUNK, T0, T1, W, true>
+                           : focus_mixed_staged_kernel<CHUNK, T0, T1, W, false>;
+        k<<<(unsigned)tiles, T0 * T1, SM::bytes, stream>>>(P, map, tb, nt0, o, ctr, status);
+        return cuda_status(cudaGetLastError(), "focus_mixed_staged launch");
+    }
+    auto *k = checksum ? focus_mixed_staged_queue_kernel<CHUNK, T0, T1, W, true>
+                       : focus_mixed_staged_queue_kernel<CHUNK, T0, T1, W, false>;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, T0 * T1, SM::bytes),
+                     "queue occupancy");
+    if (rc) return rc;
+    const int64_t grid = std::min<int64_t>(tiles, (int64_t)std::max(1, per_sm) * sms);
+    auto *cursor = reinterpret_cast<unsigned long long *>(ws + L.cursor);
+    rc = cuda_status(cudaMemsetAsync(cursor, 0, sizeof(*cursor), stream), "queue cursor reset");
+    if (rc) return rc;
+    k<<<(unsigned)grid, T0 * T1, SM::bytes, stream>>>(
+        P, map, tb, nt0, reinterpret_cast<const int32_t *>(ws + L.vals_out), tiles, cursor, o,
+        ctr, status);
+    return cuda_status(cudaGetLastError(), "focus_mixed_staged_queue launch");
 }
 
 // (chunk, tile0, tile1, window) variants the staged kernels are built for.
@@ -653,12 +709,13 @@ int launch_staged_t(const SceneParams &P, const MixedLayout &L, char *ws, double
     X(32, 16, 16, 128) X(32, 16, 16, 160) X(32, 16, 8, 128) X(32, 32, 8, 128) X(32, 64, 4, 128)
 
 int launch_staged(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L, char *ws,
-                  double *out, int32_t *nvalid, uint64_t *checksum, uint64_t *counters,
-                  cudaStream_t stream)
+                  bool queued, double *out, int32_t *nvalid, uint64_t *checksum,
+                  uint64_t *counters, cudaStream_t stream)
 {
 #define X(C, A, B, W)                                                                       \
     if (T.chunk == C && T.tile0 == A && T.tile1 == B && T.window == W)                      \
-        return launch_staged_t<C, A, B, W>(P, L, ws, out, nvalid, checksum, counters, stream);
+        return launch_staged_t<C, A, B, W>(P, L, ws, queued, out, nvalid, checksum, counters, \
+                                           stream);
     SARBP_STAGED_TILINGS(X)
 #undef X
     set_error("staged path: unsupported tuning chunk=%d tile=%dx%d window=%d", T.chunk, T.tile0,
@@ -720,10 +777,10 @@ int batch_set_scene(void *bws, size_t bytes, int slot, int nscenes, const SceneP
         set_error("batch path: slot %d outside the %d-scene workspace", slot, nscenes);
         return SARBP_EINVAL;
     }
-    const MixedLayout L = mixed_layout(P.naz, T.chunk);
-    if (!scene_ws || scene_ws_bytes < L.total || !out) {
+    const MixedLayout L = mixed_layout(P, T);
+    if (!scene_ws || scene_ws_bytes < L.base || !out) {
         set_error("batch path: scene workspace (%zu < %zu bytes) or output missing",
-                  scene_ws_bytes, L.total);
+                  scene_ws_bytes, L.base);
         return SARBP_EWORKSPACE;
     }
     BatchScene B;
@@ -839,6 +896,73 @@ int tile_costs(const SceneParams &P, const sarbp_tuning &T, int64_t *costs, cuda
 #undef X
     set_error("tile costs: unsupported tile %dx%d", T.tile0, T.tile1);
     return SARBP_EINVAL;
+}
+
+template <int T0, int T1>
+__global__ void tile_key_kernel(const SceneParams P, int64_t ntile0, int64_t ntiles,
+                                uint32_t *__restrict__ keys, int32_t *__restrict__ ids)
+{
+    const int64_t tile = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tile >= ntiles) return;
+    const int64_t t0 = tile % ntile0, t1 = tile / ntile0;
+    uint64_t c = 0;
+    for (int b = 0; b < T1; ++b)
+        for (int a = 0; a < T0; ++a) {
+            const int64_t i0 = t0 * T0 + a, i1 = t1 * T1 + b;
+            if (i0 >= P.dim0 || i1 >= P.dim1) continue;
+            const int64_t ii = i0 + P.dim0 * i1;
+            int64_t lo, hi;
+            if (pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi))
+                c += (uint64_t)(hi - lo + 1);
+        }
+    keys[tile] = c > 0xffffffffull ? 0xffffffffu : (uint32_t)c;
+    ids[tile] = (int32_t)tile;
+}
+
+size_t tile_sort_bytes(int64_t ntiles)
+{
+    size_t b = 0;
+    cub::DeviceRadixSort::SortPairsDescending((void *)nullptr, b, (const uint32_t *)nullptr,
+                                              (uint32_t *)nullptr, (const int32_t *)nullptr,
+                                              (int32_t *)nullptr, (int)ntiles);
+    return b;
+}
+
+// Tiles in decreasing estimated cost (their pixels' kept aperture lengths)
+// into the workspace queue: key kernel + device radix sort, stream-ordered.
+int tile_order(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L, char *ws,
+               cudaStream_t stream)
+{
+    const int64_t nt = L.ntiles;
+    if (nt <= 0) return SARBP_OK;
+    if (nt > 0x7fffffffLL) {
+        set_error("tile order: %lld tiles exceed the queue limit", (long long)nt);
+        return SARBP_ERANGE;
+    }
+    const int64_t nt0 = (P.dim0 + T.tile0 - 1) / T.tile0;
+    auto *keys_in = reinterpret_cast<uint32_t *>(ws + L.keys_in);
+    auto *vals_in = reinterpret_cast<int32_t *>(ws + L.vals_in);
+    const unsigned blocks = (unsigned)((nt + 127) / 128);
+    bool launched = false;
+#define X(A, B)                                                                             \
+    if (!launched && T.tile0 == A && T.tile1 == B) {                                        \
+        tile_key_kernel<A, B><<<blocks, 128, 0, stream>>>(P, nt0, nt, keys_in, vals_in);    \
+        launched = true;                                                                    \
+    }
+    X(16, 16) X(16, 8) X(32, 8) X(64, 4)
+#undef X
+    if (!launched) {
+        set_error("tile order: unsupported tile %dx%d", T.tile0, T.tile1);
+        return SARBP_EINVAL;
+    }
+    int rc = cuda_status(cudaGetLastError(), "tile_key launch");
+    if (rc) return rc;
+    size_t tmp = L.sort_tmp_bytes;
+    return cuda_status(cub::DeviceRadixSort::SortPairsDescending(
+                           ws + L.sort_tmp, tmp, keys_in,
+                           reinterpret_cast<uint32_t *>(ws + L.keys_out), vals_in,
+                           reinterpret_cast<int32_t *>(ws + L.vals_out), (int)nt, 0, 32, stream),
+                       "tile order sort");
 }
 
 int tile_count(const SceneParams &P, const sarbp_tuning &T, int64_t *nt)

@@ -82,7 +82,11 @@ extern "C" SARBP_API int sarbp_focus_mixed_noalloc(const sarbp_scene *scene,
                   (long long)P.naz, SARBP_NOALLOC_MAX_PULSES);
         return SARBP_ERANGE;
     }
-    const MixedLayout L = mixed_layout(P.naz, T.chunk);
+    MixedLayout L = mixed_layout(P, T);
+    if (T.staged == 2 && L.total > kNoAllocBytes) {
+        T.staged = 1;   // no room for the tile queue: one CTA per tile
+        L = mixed_layout(P, T);
+    }
     if (L.total > kNoAllocBytes) {
         set_error("sarbp_focus_mixed_noalloc: scene needs %zu bytes of scratch, %zu built in",
                   L.total, kNoAllocBytes);

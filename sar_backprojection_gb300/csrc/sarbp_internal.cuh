@@ -107,15 +107,23 @@ bool build_params(const sarbp_scene *s, SceneParams *p);
 int cuda_status(cudaError_t e, const char *what);
 bool valid_tuning(sarbp_tuning *t);   // fills library defaults, validates
 
-// Mixed-path workspace layout (offsets 256-byte aligned).
+// Mixed-path workspace layout (offsets 256-byte aligned).  The first part
+// (up to `base`) is the chunk tables every mixed launch needs; staged=2
+// adds the cost-ordered tile queue its persistent grid drains (up to
+// `total`; total == base otherwise).
 struct MixedLayout {
     size_t status;   // StatusBlock
-    size_t ptab;     // float4[naz]: e = t(k) - t(k0), |e|^2
+    size_t ptab;     // float4[nchunks*chunk]: e = t(k) - t(k0), |e|^2
     size_t pff;      // PulseFF[naz]: float-float pulse positions
     size_t ctab;     // ChunkRef[nchunks]: bounds of e and t(k0)
+    size_t base;     // end of the chunk tables
+    int64_t ntiles;  // staged=2: pixel tiles of the scene (0 otherwise)
+    size_t keys_in, vals_in, keys_out, vals_out;   // tile costs / ids, sorted
+    size_t sort_tmp, sort_tmp_bytes;               // radix-sort scratch
+    size_t cursor;   // queue cursor (unsigned long long)
     size_t total;
 };
-MixedLayout mixed_layout(int64_t naz, int chunk);
+MixedLayout mixed_layout(const SceneParams &P, const sarbp_tuning &T);
 
 int launch_focus_fp64(const SceneParams &P, double *out, int32_t *nvalid, uint64_t *checksum,
                       cudaStream_t stream);
@@ -135,5 +143,8 @@ int batch_set_items(void *bws, size_t bytes, int nscenes, const int32_t *items, 
 int batch_focus(void *bws, size_t bytes, int nscenes, const sarbp_tuning &T, int64_t n_items,
                 bool diag, uint64_t *counters, cudaStream_t stream);
 int tile_costs(const SceneParams &P, const sarbp_tuning &T, int64_t *costs, cudaStream_t stream);
+int tile_order(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L, char *ws,
+               cudaStream_t stream);
+size_t tile_sort_bytes(int64_t ntiles);
 int tile_count(const SceneParams &P, const sarbp_tuning &T, int64_t *nt);
 }  // namespace sarbp

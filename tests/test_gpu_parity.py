@@ -27,11 +27,13 @@ MIXED_REL_L2 = 1e-3
 
 TUNINGS = ([dict(chunk=c, tile0=t0, tile1=t1, staged=0) for c in (32, 64)
             for (t0, t1) in ((32, 8), (64, 4), (16, 16))]
-           + [dict(chunk=32, tile0=t0, tile1=t1, staged=1, window=w)
+           + [dict(chunk=32, tile0=t0, tile1=t1, staged=s, window=w)
+              for s in (1, 2)
               for (t0, t1, w) in ((32, 8, 128), (64, 4, 128), (16, 16, 128), (16, 16, 160),
                                   (16, 8, 128))])
 TUNING_IDS = [f"c{t['chunk']}_{t['tile0']}x{t['tile1']}_"
-              + (f"tma{t['window']}" if t['staged'] else "l1") for t in TUNINGS]
+              + ({0: "l1", 1: "tma", 2: "queue"}[t['staged']])
+              + (str(t['window']) if t['staged'] else "") for t in TUNINGS]
 
 
 def run(scene, precision, tuning=None):
@@ -147,9 +149,11 @@ def test_full_workload_fp64(full_scene, full_oracle):
                                     dict(chunk=32, tile0=16, tile1=16, staged=1, window=128),
                                     dict(chunk=32, tile0=16, tile1=16, staged=1, window=160),
                                     dict(chunk=32, tile0=16, tile1=8, staged=1, window=128),
-                                    dict(chunk=32, tile0=64, tile1=4, staged=1, window=128)],
+                                    dict(chunk=32, tile0=64, tile1=4, staged=1, window=128),
+                                    dict(chunk=32, tile0=16, tile1=16, staged=2, window=160),
+                                    dict(chunk=32, tile0=16, tile1=8, staged=2, window=128)],
                          ids=["c64_l1", "tma_16x16w128", "tma_16x16w160", "tma_16x8w128",
-                              "tma_64x4w128"])
+                              "tma_64x4w128", "queue_16x16w160", "queue_16x8w128"])
 def test_full_workload_mixed(full_scene, full_oracle, tuning):
     """Mixed kernel variants against the full oracle image."""
     oimg, onv, ocs = full_oracle
@@ -160,3 +164,14 @@ def test_full_workload_mixed(full_scene, full_oracle, tuning):
     print("full workload mixed", tuning, {k: q[k] for k in ("rel_l2", "coherence",
                                                              "rms_phase_mrad")},
           "counters:", ctr[:4])
+
+
+@pytest.mark.parametrize("tiling", [(16, 16, 160), (32, 8, 128)], ids=["16x16w160", "32x8w128"])
+def test_tile_queue_matches_one_cta_per_tile(full_scene, tiling):
+    """The persistent queue grid runs the same per-tile code: bit-identical."""
+    t0, t1, w = tiling
+    a = run(full_scene, "mixed", dict(chunk=32, tile0=t0, tile1=t1, staged=1, window=w))
+    b = run(full_scene, "mixed", dict(chunk=32, tile0=t0, tile1=t1, staged=2, window=w))
+    for x, y in zip(a[:3], b[:3]):
+        assert np.array_equal(x, y)
+    assert np.array_equal(a[3][:3], b[3][:3]) and b[3][3] == 0
