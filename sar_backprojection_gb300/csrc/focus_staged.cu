@@ -532,6 +532,7 @@ focus_mixed_staged_queue_kernel(const SceneParams P, const __grid_constant__ CUt
         const long long item = s_item[round & 1];
         if (item >= ntiles) break;
         const int64_t tile = order[item];
+        if (tile < 0 || tile >= ntiles) continue;   // a queue prepared for other pixels
         const bool ok = staged_tile<CHUNK, T0, T1, W, kChecksum>(
             cta, P, &raw_map, tb, tile % ntile0, tile / ntile0, o, st);
         if (!ok) {

@@ -147,6 +147,10 @@ class LargeSceneFocuser:
         self.batch_cols = int(batch_cols)
         self.device = torch.device(device or "cuda")
         self.tuning = resolve_tuning(tuning)
+        # one prepared workspace serves every batch: its chunk tables depend
+        # on the trajectory only, a tile queue (staged=2) on one batch's pixels
+        if self.tuning.staged == 2:
+            self.tuning.staged = 1
         self.block_pulses = block_pulses
         self.lib = _lib.load()
         self.launches = 0

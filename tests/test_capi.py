@@ -91,7 +91,14 @@ def test_workspace_size_is_host_only():
     s.nra, s.naz, s.raw_pitch = 4762, 40001, 4762
     s.delta_range, s.lambda_, s.near_range = 0.5, 0.031, 3500.0
     t = _lib.default_tuning()
+    assert t.staged == 1
     n = lib.sarbp_mixed_workspace_size(C.byref(s), C.byref(t))
     assert n >= 16 * 40001
+    t.staged = 2                               # + the tile queue: 4 arrays of 4000 tiles
+    assert lib.sarbp_mixed_workspace_size(C.byref(s), C.byref(t)) >= n + 16 * 4000
+    t.staged = 3
+    assert lib.sarbp_mixed_workspace_size(C.byref(s), C.byref(t)) == _lib.SARBP_EINVAL
+    assert "staged" in _lib.last_error()
+    t.staged = 1
     t.chunk = 48
     assert lib.sarbp_mixed_workspace_size(C.byref(s), C.byref(t)) == _lib.SARBP_EINVAL
