@@ -29,6 +29,8 @@ MixedLayout mixed_layout(const SceneParams &P, const sarbp_tuning &T)
     off = align256(off + sizeof(PulseFF) * (size_t)naz);
     L.ctab = off;
     off = align256(off + sizeof(ChunkRef) * (size_t)nchunks);
+    L.sdev = off;
+    off = align256(off + sizeof(float) * (size_t)(nchunks * chunk / 32));
     L.base = off;
     if (T.staged == 2 && T.tile0 > 0 && T.tile1 > 0) {
         const int64_t nt = ((P.dim0 + T.tile0 - 1) / T.tile0) * ((P.dim1 + T.tile1 - 1) / T.tile1);
@@ -60,7 +62,7 @@ __host__ __device__ __forceinline__ int64_t chunk_ref(int64_t c, int chunk, int6
 // Per-pulse tables and per-chunk references; one warp per chunk.
 __global__ void chunk_table_kernel(const SceneParams P, int chunk, float4 *__restrict__ ptab,
                                    PulseFF *__restrict__ pff, ChunkRef *__restrict__ ctab,
-                                   int64_t nchunks)
+                                   float *__restrict__ sdev, int64_t nchunks)
 {
     const int64_t c = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     const int lane = threadIdx.x & 31;
@@ -105,6 +107,27 @@ __global__ void chunk_table_kernel(const SceneParams P, int chunk, float4 *__res
         const double u = ss > 0.0 ? (qx * sx + qy * sy + qz * sz) / ss : 0.0;
         const double rx = qx - u * sx, ry = qy - u * sy, rz = qz - u * sz;
         dev = fmax(dev, sqrt(rx * rx + ry * ry + rz * rz));
+    }
+    // The same per 32-pulse stage (the staged kernel's TMA unit): one pulse
+    // per lane.
+    for (int s = 0; s < chunk / 32; ++s) {
+        const int64_t sa = c * chunk + s * 32;
+        double sd = 0.0;
+        if (sa < P.naz) {
+            const int64_t sb = min(sa + 31, P.naz - 1);
+            const double bx = P.tx[sa], by = P.ty[sa], bz = P.tz[sa];
+            const double vx = P.tx[sb] - bx, vy = P.ty[sb] - by, vz = P.tz[sb] - bz;
+            const double vv = vx * vx + vy * vy + vz * vz;
+            const int64_t k = sa + lane;
+            if (k <= sb) {
+                const double qx = P.tx[k] - bx, qy = P.ty[k] - by, qz = P.tz[k] - bz;
+                const double u = vv > 0.0 ? (qx * vx + qy * vy + qz * vz) / vv : 0.0;
+                const double rx = qx - u * vx, ry = qy - u * vy, rz = qz - u * vz;
+                sd = sqrt(rx * rx + ry * ry + rz * rz);
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) sd = fmax(sd, __shfl_xor_sync(0xffffffffu, sd, o));
+        if (lane == 0) sdev[c * (chunk / 32) + s] = (float)sd + 1.0e-3f;   // + margin (m)
     }
     for (int o = 16; o > 0; o >>= 1) {
         mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -304,7 +327,7 @@ int launch_chunk_table(const SceneParams &P, int chunk, char *ws, const MixedLay
     const int64_t blocks = (nchunks + warps - 1) / warps;
     chunk_table_kernel<<<(unsigned)blocks, warps * 32, 0, stream>>>(
         P, chunk, reinterpret_cast<float4 *>(ws + L.ptab), reinterpret_cast<PulseFF *>(ws + L.pff),
-        reinterpret_cast<ChunkRef *>(ws + L.ctab), nchunks);
+        reinterpret_cast<ChunkRef *>(ws + L.ctab), reinterpret_cast<float *>(ws + L.sdev), nchunks);
     return cuda_status(cudaGetLastError(), "chunk_table launch");
 }
 

@@ -2,18 +2,24 @@
 // windows.
 //
 // Same decomposition and precision plan as the gather kernel
-// (focus_mixed.cu, mixed_common.cuh), but each CTA stages, per pulse chunk,
-// the range window its pixel tile can touch into shared memory with one 2-D
-// tiled TMA load (box = W range bins x CHUNK pulses of the pulse-major raw
-// data) plus a 1-D bulk copy of the chunk's per-pulse table, double
-// buffered: while the CTA focuses chunk c from stage c&1, the copies of chunk
-// c+1 land in the other stage.  The per-pulse gathers then hit shared memory
-// instead of L1/L2.
+// (focus_mixed.cu, mixed_common.cuh), but each CTA stages, per 32-pulse
+// stage, the range window its pixel tile can touch into shared memory with
+// one 2-D tiled TMA load (box = W range bins x 32 pulses of the pulse-major
+// raw data) plus a 1-D bulk copy of the stage's per-pulse table, double
+// buffered: while the CTA focuses stage c from buffer c&1, the copies of
+// stage c+1 land in the other buffer.  The per-pulse gathers then hit shared
+// memory instead of L1/L2.
 //
-// The window of chunk c is the range-bin interval every pixel of the tile can
-// reach from the chunk's pulses: per pixel, the distances to the chunk's
+// The float-float reference (chunk_setup) is computed once per chunk of
+// CHUNK = 32 or 64 pulses (reference pulse mid-chunk, so |e| <= 16 m for
+// either), before the wait for the chunk's first stage; a chunk's stages sum
+// into one FP32 partial that is rotated by the reference phasor and added to
+// the Kahan accumulator once per chunk.
+//
+// The window of stage c is the range-bin interval every pixel of the tile can
+// reach from the stage's pulses: per pixel, the distances to the stage's
 // first and last pulse positions (maximum) and to the chord between them
-// (minimum), widened by the chunk's deviation from that chord and one bin on
+// (minimum), widened by the stage's deviation from that chord and one bin on
 // each side; reduced over the tile in a prologue.  A bin outside the staged
 // window (a window wider than W) is read from global memory instead and
 // counted as a window miss, so correctness never depends on the window.
@@ -35,13 +41,15 @@
 
 namespace sarbp {
 
-constexpr int kMaxPassChunks = 128;        // chunks whose windows are kept at once
+constexpr int kStage = 32;                 // pulses per TMA stage
+constexpr int kMaxPassChunks = 128;        // stages whose windows are kept at once
 constexpr uint32_t kWaitLimit = 1u << 22;  // mbarrier polls before giving up
 
 template <int CHUNK, int W>
 struct StagedSmem {
-    static constexpr size_t raw_bytes = (size_t)CHUNK * W * sizeof(float2);
-    static constexpr size_t tab_bytes = (size_t)CHUNK * sizeof(float4);
+    static_assert(CHUNK % kStage == 0 && kMaxPassChunks % (CHUNK / kStage) == 0, "chunk");
+    static constexpr size_t raw_bytes = (size_t)kStage * W * sizeof(float2);
+    static constexpr size_t tab_bytes = (size_t)kStage * sizeof(float4);
     static constexpr size_t stage_bytes = raw_bytes + tab_bytes;
     static constexpr size_t bytes = 2 * stage_bytes + 128;    // + alignment slack
 };
@@ -114,6 +122,7 @@ struct TileTables {
     const float4 *ptab;
     const PulseFF *pff;
     const ChunkRef *ctab;
+    const float *sdev;
 };
 
 struct TileOutputs {
@@ -150,6 +159,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
     const float4 *ptab = tb.ptab;
     const PulseFF *pff = tb.pff;
     const ChunkRef *ctab = tb.ctab;
+    const float *sdev = tb.sdev;
 
     const int t = threadIdx.x;
     int64_t i0, i1;
@@ -184,23 +194,29 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
     bool *pending = cta.pending;
     uint32_t *pending_parity = cta.pending_parity;
     bool aborted = false;
+    constexpr int R = CHUNK / kStage;     // stages per chunk (setup group)
+    ChunkSetup S;
+    safe_setup(S, 0);
+    bool gwork = false;                   // pixel has pulses in the current chunk
+    int64_t cur_chunk = -1;
+    float gre = 0.f, gim = 0.f;           // FP32 partial sum of the current chunk
     if (thi >= 0) {
-        const int64_t c_first = tlo / CHUNK, c_last = thi / CHUNK;
+        const int64_t c_first = tlo / kStage, c_last = thi / kStage;
         for (int64_t cb = c_first; cb <= c_last && !aborted; cb += kMaxPassChunks) {
             const int npass = (int)min((int64_t)kMaxPassChunks, c_last - cb + 1);
-            // ---- window prologue: bins every pixel can reach per chunk ----
+            // ---- window prologue: bins every pixel can reach per stage ----
             for (int q = t; q < npass; q += blockDim.x) {
                 s_wlo[q] = INT_MAX;
                 s_whi[q] = INT_MIN;
             }
             __syncthreads();
             for (int q = 0; q < npass; ++q) {
-                const int64_t K = (cb + q) * CHUNK;
+                const int64_t K = (cb + q) * kStage;
                 int blo = INT_MAX, bhi = INT_MIN;
-                if (active && lo <= K + CHUNK - 1 && hi >= K) {
-                    const int64_t ka = K, kb = min(K + CHUNK - 1, P.naz - 1);
+                if (active && lo <= K + kStage - 1 && hi >= K) {
+                    const int64_t ka = K, kb = min(K + kStage - 1, P.naz - 1);
                     const float4 ta = __ldg(&pff[ka].hi), tb = __ldg(&pff[kb].hi);
-                    const float dev = __ldg(&ctab[cb + q].thi.w);
+                    const float dev = __ldg(&sdev[cb + q]);
                     const float ax = pf.xh - ta.x, ay = pf.yh - ta.y, az = pf.zh - ta.z;
                     const float bx = pf.xh - tb.x, by = pf.yh - tb.y, bz = pf.zh - tb.z;
                     const float ra = sqrtf(ax * ax + ay * ay + az * az);
@@ -227,9 +243,9 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
             }
             __syncthreads();
 
-            // ---- producer: stage chunk q of this pass into stage s ----
-            // window start of chunk q: even (16-byte aligned TMA x coordinate),
-            // inside [0, nra]; 0 for a chunk no pixel of the tile reaches
+            // ---- producer: stage q of this pass into buffer s ----
+            // window start of stage q: even (16-byte aligned TMA x coordinate),
+            // inside [0, nra]; 0 for a stage no pixel of the tile reaches
             auto window_start = [&](int q) {
                 const int wl = s_wlo[q], wh = s_whi[q];
                 if (wl > wh) return 0;
@@ -237,7 +253,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
             };
             auto issue = [&](int q, int s, uint32_t use) {
                 unsigned char *base = smem + (size_t)s * SM::stage_bytes;
-                const int64_t K = (cb + q) * CHUNK;
+                const int64_t K = (cb + q) * kStage;
                 mbar_arrive_expect_tx(&full_bar[s], (uint32_t)SM::stage_bytes);
                 tma_load_2d(base, raw_map, &full_bar[s], window_start(q), (int)K);
                 bulk_load(base + SM::raw_bytes, ptab + K, (uint32_t)SM::tab_bytes, &full_bar[s]);
@@ -249,13 +265,31 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
             for (int q = 0; q < npass; ++q, ++it) {
                 const int s = it & 1;
                 if (t == 0 && q + 1 < npass) issue(q + 1, s ^ 1, (it + 1) >> 1);
+                const int64_t c = cb + q;
+                const int64_t K = c * kStage;
+                // ---- chunk reference: once per CHUNK pulses, before the wait ----
+                const int64_t chunk = c / R;
+                if (chunk != cur_chunk) {
+                    cur_chunk = chunk;
+                    const int64_t C0 = chunk * CHUNK;
+                    gwork = active && lo <= C0 + CHUNK - 1 && hi >= C0;
+                    gre = gim = 0.f;
+                    if (gwork) {
+                        ++chunks;
+                        ChunkRef ref;
+                        ref.emax = __ldg(&ctab[chunk].emax);
+                        ref.thi = __ldg(&ctab[chunk].thi);
+                        ref.tlo = __ldg(&ctab[chunk].tlo);
+                        chunk_setup(P, pf, ref, S);
+                    } else {
+                        safe_setup(S, 0);
+                    }
+                }
                 const bool ready = mbar_wait(&full_bar[s], (it >> 1) & 1, kWaitLimit);
                 if (t == 0 && ready) pending[s] = false;
-                const int64_t c = cb + q;
-                const int64_t K = c * CHUNK;
                 const int jmin = (int)(lo > K ? lo - K : 0);
-                const int jmax = (int)(hi < K + CHUNK - 1 ? hi - K : CHUNK - 1);
-                const bool work = ready && active && jmin <= jmax;
+                const int jmax = (int)(hi < K + kStage - 1 ? hi - K : kStage - 1);
+                const bool work = ready && gwork && jmin <= jmax;
                 const float2 *sraw =
                     reinterpret_cast<const float2 *>(smem + (size_t)s * SM::stage_bytes);
                 const float4 *stab = reinterpret_cast<const float4 *>(
@@ -265,22 +299,12 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                 // the kept bins 0..nra-2: no per-pulse validity/window tests
                 const bool win_ok = s_wlo[q] >= 0 && (int64_t)s_whi[q] <= P.nra - 2 &&
                                     s_whi[q] - b0 < W;
-                ChunkSetup S;
-                safe_setup(S, b0);                 // lanes without work read column 0
-                if (work) {
-                    ++chunks;
-                    ChunkRef ref;
-                    ref.emax = __ldg(&ctab[c].emax);
-                    ref.thi = __ldg(&ctab[c].thi);
-                    ref.tlo = __ldg(&ctab[c].tlo);
-                    chunk_setup(P, pf, ref, S);
-                }
                 const bool exact = work && S.exact;
                 const bool fast = __all_sync(0xffffffffu, !work || (jmin == 0 &&
-                                                                    jmax == CHUNK - 1 &&
+                                                                    jmax == kStage - 1 &&
                                                                     win_ok && !exact));
                 if (!__any_sync(0xffffffffu, work)) {
-                    // no pixel of this warp has pulses in the chunk
+                    // no pixel of this warp has pulses in the stage
                 } else if (exact) {
                     const double px = P.x[ii], py = P.y[ii], pz = P.z[ii];
                     double sre = 0.0, sim = 0.0;
@@ -297,14 +321,16 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                     kahan_add(acc_re, cmp_re, (float)sre);
                     kahan_add(acc_im, cmp_im, (float)sim);
                 } else {
+                    // lanes without work use their (zero or other-chunk) setup
+                    // and read column 0 or a clamped column; nothing is added
                     const int colbias = S.n0 - b0 - 0x4B400000;
                     const float tie = 0.5f - S.eps;
-                    float sre = 0.f, sim = 0.f;
+                    float sre = gre, sim = gim;
                     uint32_t amb_mask = 0, miss_mask = 0, valid_mask;
                     if (fast) {
                         valid_mask = 0xffffffffu;
 #pragma unroll
-                        for (int j = 0; j < CHUNK; ++j) {
+                        for (int j = 0; j < kStage; ++j) {
                             float D, dR;
                             int col;
                             bool amb;
@@ -325,7 +351,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                                     ~((1u << jmin) - 1u))
                                  : 0u;
 #pragma unroll
-                        for (int j = 0; j < CHUNK; ++j) {
+                        for (int j = 0; j < kStage; ++j) {
                             float D, dR;
                             int col;
                             bool amb;
@@ -397,13 +423,19 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                             }
                         }
                         n += __popc(valid_mask);
-                        const float rre = fmaf(sre, S.w0re, -(sim * S.w0im));
-                        const float rim = fmaf(sre, S.w0im, sim * S.w0re);
-                        kahan_add(acc_re, cmp_re, rre);
-                        kahan_add(acc_im, cmp_im, rim);
+                        gre = sre;
+                        gim = sim;
                     }
                 }
-                // every thread is done with stage s before it is refilled
+                // end of the chunk: rotate its partial by the reference phasor
+                if (gwork && !S.exact && (c % R == R - 1 || c == c_last)) {
+                    const float rre = fmaf(gre, S.w0re, -(gim * S.w0im));
+                    const float rim = fmaf(gre, S.w0im, gim * S.w0re);
+                    kahan_add(acc_re, cmp_re, rre);
+                    kahan_add(acc_im, cmp_im, rim);
+                    gre = gim = 0.f;
+                }
+                // every thread is done with buffer s before it is refilled
                 if (__syncthreads_or(!ready)) {
                     aborted = true;
                     break;
@@ -598,7 +630,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 
 // 2-D tensor map over the pulse-major raw data: dim0 = range bins (8-byte
 // complex64 elements), dim1 = pulses; box = W bins x CHUNK pulses.
-static int make_raw_map(const SceneParams &P, int W, int chunk, CUtensorMap *map)
+static int make_raw_map(const SceneParams &P, int W, int rows, CUtensorMap *map)
 {
     auto enc = tensor_map_encoder();
     if (!enc) {
@@ -613,7 +645,7 @@ static int make_raw_map(const SceneParams &P, int W, int chunk, CUtensorMap *map
     }
     cuuint64_t dims[2] = {(cuuint64_t)P.nra, (cuuint64_t)P.naz};
     cuuint64_t strides[1] = {(cuuint64_t)P.pitch * 8};
-    cuuint32_t box[2] = {(cuuint32_t)W, (cuuint32_t)chunk};
+    cuuint32_t box[2] = {(cuuint32_t)W, (cuuint32_t)rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<float2 *>(P.raw), dims,
                      strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -657,6 +689,7 @@ static TileTables tables_of(char *ws, const MixedLayout &L)
     tb.ptab = reinterpret_cast<const float4 *>(ws + L.ptab);
     tb.pff = reinterpret_cast<const PulseFF *>(ws + L.pff);
     tb.ctab = reinterpret_cast<const ChunkRef *>(ws + L.ctab);
+    tb.sdev = reinterpret_cast<const float *>(ws + L.sdev);
     return tb;
 }
 
@@ -673,7 +706,7 @@ int launch_staged_t(const SceneParams &P, const MixedLayout &L, char *ws, bool q
         return SARBP_ERANGE;
     }
     CUtensorMap map;
-    int rc = make_raw_map(P, W, CHUNK, &map);
+    int rc = make_raw_map(P, W, kStage, &map);
     if (rc) return rc;
     rc = ensure_smem_attr<CHUNK, T0, T1, W>();
     if (rc) return rc;
@@ -707,7 +740,8 @@ int launch_staged_t(const SceneParams &P, const MixedLayout &L, char *ws, bool q
 
 // (chunk, tile0, tile1, window) variants the staged kernels are built for.
 #define SARBP_STAGED_TILINGS(X) \
-    X(32, 16, 16, 128) X(32, 16, 16, 160) X(32, 16, 8, 128) X(32, 32, 8, 128) X(32, 64, 4, 128)
+    X(32, 16, 16, 128) X(32, 16, 16, 160) X(32, 16, 8, 128) X(32, 32, 8, 128) X(32, 64, 4, 128) \
+    X(64, 16, 16, 128) X(64, 16, 16, 160) X(64, 16, 8, 128) X(64, 32, 8, 128) X(64, 64, 4, 128)
 
 int launch_staged(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L, char *ws,
                   bool queued, double *out, int32_t *nvalid, uint64_t *checksum,
@@ -769,8 +803,8 @@ int batch_set_scene(void *bws, size_t bytes, int slot, int nscenes, const SceneP
                     const sarbp_tuning &T, void *scene_ws, size_t scene_ws_bytes, double *out,
                     int32_t *nvalid, uint64_t *checksum, cudaStream_t stream)
 {
-    if (!T.staged || T.chunk != 32) {
-        set_error("batch path: needs the staged kernel with 32-pulse chunks");
+    if (!T.staged || (T.chunk != 32 && T.chunk != 64)) {
+        set_error("batch path: needs the staged kernel with 32- or 64-pulse chunks");
         return SARBP_EINVAL;
     }
     const BatchLayout BL = batch_layout(nscenes, 0);
@@ -786,7 +820,7 @@ int batch_set_scene(void *bws, size_t bytes, int slot, int nscenes, const SceneP
     }
     BatchScene B;
     memset(&B, 0, sizeof(B));
-    int rc = make_raw_map(P, T.window, T.chunk, &B.map);
+    int rc = make_raw_map(P, T.window, kStage, &B.map);
     if (rc) return rc;
     B.P = P;
     B.tables = tables_of(static_cast<char *>(scene_ws), L);

@@ -116,6 +116,7 @@ struct MixedLayout {
     size_t ptab;     // float4[nchunks*chunk]: e = t(k) - t(k0), |e|^2
     size_t pff;      // PulseFF[naz]: float-float pulse positions
     size_t ctab;     // ChunkRef[nchunks]: bounds of e and t(k0)
+    size_t sdev;     // float[nchunks*chunk/32]: chord deviation per 32-pulse stage
     size_t base;     // end of the chunk tables
     int64_t ntiles;  // staged=2: pixel tiles of the scene (0 otherwise)
     size_t keys_in, vals_in, keys_out, vals_out;   // tile costs / ids, sorted
