@@ -120,8 +120,8 @@ bool valid_tuning(sarbp_tuning *t)
         set_error("tuning.staged must be 0, 1 or 2 (got %d)", t->staged);
         return false;
     }
-    if (t->chunk != 32 && t->chunk != 64) {
-        set_error("tuning.chunk must be 32 or 64 (got %d)", t->chunk);
+    if (t->chunk != 32 && t->chunk != 64 && !(t->staged && t->chunk == 128)) {
+        set_error("tuning.chunk must be 32 or 64 (or 128 with staged > 0; got %d)", t->chunk);
         return false;
     }
     return true;

@@ -1,616 +1,16 @@
-// focus_staged.cu -- mixed-precision back-projection with TMA-staged raw
-// windows.
-//
-// Same decomposition and precision plan as the gather kernel
-// (focus_mixed.cu, mixed_common.cuh), but each CTA stages, per 32-pulse
-// stage, the range window its pixel tile can touch into shared memory with
-// one 2-D tiled TMA load (box = W range bins x 32 pulses of the pulse-major
-// raw data) plus a 1-D bulk copy of the stage's per-pulse table, double
-// buffered: while the CTA focuses stage c from buffer c&1, the copies of
-// stage c+1 land in the other buffer.  The per-pulse gathers then hit shared
-// memory instead of L1/L2.
-//
-// The float-float reference (chunk_setup) is computed once per chunk of
-// CHUNK = 32 or 64 pulses (reference pulse mid-chunk, so |e| <= 16 m for
-// either), before the wait for the chunk's first stage; a chunk's stages sum
-// into one FP32 partial that is rotated by the reference phasor and added to
-// the Kahan accumulator once per chunk.
-//
-// The window of stage c is the range-bin interval every pixel of the tile can
-// reach from the stage's pulses: per pixel, the distances to the stage's
-// first and last pulse positions (maximum) and to the chord between them
-// (minimum), widened by the stage's deviation from that chord and one bin on
-// each side; reduced over the tile in a prologue.  A bin outside the staged
-// window (a window wider than W) is read from global memory instead and
-// counted as a window miss, so correctness never depends on the window.
-//
-// All mbarrier waits are bounded; a wait that gives up marks the workspace
-// status block and the CTA leaves after its last copy lands (or after a
-// second bounded wait).
+// focus_staged.cu -- host side of the TMA-staged kernels: tensor maps,
+// per-chunk-size dispatch, batch workspaces, tile cost and queue order.
+// The kernels and their launch templates are in staged_kernels.cuh.
 #include <algorithm>
 #include <climits>
 #include <cstdio>
 #include <cstring>
 
 #include <cub/device/device_radix_sort.cuh>
-#include <cuda.h>
-#include <cudaTypedefs.h>
 
-#include "mixed_common.cuh"
-#include "tma.cuh"
+#include "staged_kernels.cuh"
 
 namespace sarbp {
-
-constexpr int kStage = 32;                 // pulses per TMA stage
-constexpr int kMaxPassChunks = 128;        // stages whose windows are kept at once
-constexpr uint32_t kWaitLimit = 1u << 22;  // mbarrier polls before giving up
-
-template <int CHUNK, int W>
-struct StagedSmem {
-    static_assert(CHUNK % kStage == 0 && kMaxPassChunks % (CHUNK / kStage) == 0, "chunk");
-    static constexpr size_t raw_bytes = (size_t)kStage * W * sizeof(float2);
-    static constexpr size_t tab_bytes = (size_t)kStage * sizeof(float4);
-    static constexpr size_t stage_bytes = raw_bytes + tab_bytes;
-    static constexpr size_t bytes = 2 * stage_bytes + 128;    // + alignment slack
-};
-
-template <int T0, int T1>
-__device__ __forceinline__ void staged_tile_pixel(int t, int64_t tile0, int64_t tile1,
-                                                  int64_t &i0, int64_t &i1)
-{
-    static_assert(T0 % 8 == 0 && T1 % 4 == 0, "tile must be a multiple of the 8x4 warp block");
-    const int w = t >> 5, lane = t & 31;
-    i0 = tile0 * T0 + (w % (T0 / 8)) * 8 + (lane & 7);
-    i1 = tile1 * T1 + (w / (T0 / 8)) * 4 + (lane >> 3);
-}
-
-// FP32 per-pulse range geometry: D = R^2 - R0^2, dR = R - R0, the window
-// column of the FP32 range bin, and whether that bin is within the tie band.
-__device__ __forceinline__ void pulse_eval(const ChunkSetup &S, float4 e, float inv_dra,
-                                           int colbias, float tie, float &D, float &dR,
-                                           int &col, bool &amb)
-{
-    D = fmaf(S.mx, e.x, fmaf(S.my, e.y, fmaf(S.mz, e.z, e.w)));
-    dR = D * fmaf(fmaf(S.c3, D, S.c2), D, S.c1);
-    const float g = fmaf(dR, inv_dra, S.g0);
-    const float t = __fadd_rn(g, 12582912.0f);
-    col = __float_as_int(t) + colbias;
-    amb = fabsf(__fsub_rn(g, __fsub_rn(t, 12582912.0f))) > tie;
-}
-
-// R^2 * exp(-j*dphi) as (wc, ws): term = (vx + j*vy) * (wc - j*ws).
-__device__ __forceinline__ void pulse_phasor(const ChunkSetup &S, float D, float dR, float beta,
-                                             float &wc, float &ws)
-{
-    const float ph = dR * fmaf(beta, dR, S.a);
-    float sn, cn;
-    __sincosf(ph, &sn, &cn);
-    const float w = S.r0sq + D;
-    wc = w * cn;
-    ws = w * sn;
-}
-
-// Setup of a lane without work in this chunk: every pulse maps to column 0.
-__device__ __forceinline__ void safe_setup(ChunkSetup &S, int b0)
-{
-    S.mx = S.my = S.mz = 0.f;
-    S.c1 = S.c2 = S.c3 = 0.f;
-    S.g0 = 0.f;
-    S.a = 0.f;
-    S.r0sq = 0.f;
-    S.w0re = 1.f;
-    S.w0im = 0.f;
-    S.eps = 0.f;
-    S.n0 = b0;
-    S.exact = false;
-}
-
-// Shared-memory state of one CTA of a staged kernel.  It persists across the
-// tiles a persistent CTA processes: the stage counter keeps the mbarrier
-// phases in step.
-struct StagedCta {
-    unsigned char *smem;       // 2 stages, 1024-byte aligned
-    uint64_t *full_bar;        // [2] copy-completion barriers
-    int *s_wlo, *s_whi;        // [kMaxPassChunks] range windows of a pass
-    long long *s_lo, *s_hi;    // tile-wide pulse range
-    uint32_t it;               // chunk iteration counter (stage = it & 1)
-    bool pending[2];           // thread 0: copies in flight per stage
-    uint32_t pending_parity[2];
-};
-
-struct TileTables {
-    const float4 *ptab;
-    const PulseFF *pff;
-    const ChunkRef *ctab;
-    const float *sdev;
-};
-
-struct TileOutputs {
-    double2 *out;
-    int32_t *nvalid;
-    uint64_t *checksum;
-};
-
-struct TileStats {
-    unsigned ambiguous, chunks, misses;
-};
-
-// One scene of a batch, as the persistent kernel reads it from device memory.
-struct BatchScene {
-    CUtensorMap map;          // raw-data window tensor map (64-byte aligned)
-    SceneParams P;
-    TileTables tables;
-    TileOutputs outputs;
-    int64_t ntile0, ntiles;
-};
-
-// Focus one pixel tile; false if a bounded wait gave up (the CTA must stop).
-// Every thread of the CTA calls it with the same tile.
-template <int CHUNK, int T0, int T1, int W, bool kChecksum>
-__device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P,
-                                            const CUtensorMap *raw_map, const TileTables &tb,
-                                            int64_t tile0, int64_t tile1, const TileOutputs &o,
-                                            TileStats &st)
-{
-    using SM = StagedSmem<CHUNK, W>;
-    unsigned char *smem = cta.smem;
-    uint64_t *full_bar = cta.full_bar;
-    int *s_wlo = cta.s_wlo, *s_whi = cta.s_whi;
-    const float4 *ptab = tb.ptab;
-    const PulseFF *pff = tb.pff;
-    const ChunkRef *ctab = tb.ctab;
-    const float *sdev = tb.sdev;
-
-    const int t = threadIdx.x;
-    int64_t i0, i1;
-    staged_tile_pixel<T0, T1>(t, tile0, tile1, i0, i1);
-    const bool inside = i0 < P.dim0 && i1 < P.dim1;
-    const int64_t ii = inside ? i0 + P.dim0 * i1 : 0;
-    int64_t lo = 0, hi = -1;
-    const bool active =
-        inside && pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi);
-
-    if (t == 0) {
-        *cta.s_lo = LLONG_MAX;
-        *cta.s_hi = -1;
-    }
-    __syncthreads();
-    if (active) {
-        atomicMin(cta.s_lo, (long long)lo);
-        atomicMax(cta.s_hi, (long long)hi);
-    }
-    __syncthreads();
-    const int64_t tlo = *cta.s_lo, thi = *cta.s_hi;
-
-    PixelFF pf{};
-    if (active) pf = pixel_ff(P.x[ii], P.y[ii], P.z[ii]);
-    float acc_re = 0.f, acc_im = 0.f, cmp_re = 0.f, cmp_im = 0.f;
-    int n = 0;
-    uint64_t cs = 0;
-    unsigned ambiguous = 0, chunks = 0, misses = 0;
-    const unsigned nra_m1 = (unsigned)(P.nra - 1);
-    const int pitch = (int)P.pitch;
-    uint32_t &it = cta.it;
-    bool *pending = cta.pending;
-    uint32_t *pending_parity = cta.pending_parity;
-    bool aborted = false;
-    constexpr int R = CHUNK / kStage;     // stages per chunk (setup group)
-    ChunkSetup S;
-    safe_setup(S, 0);
-    bool gwork = false;                   // pixel has pulses in the current chunk
-    int64_t cur_chunk = -1;
-    float gre = 0.f, gim = 0.f;           // FP32 partial sum of the current chunk
-    if (thi >= 0) {
-        const int64_t c_first = tlo / kStage, c_last = thi / kStage;
-        for (int64_t cb = c_first; cb <= c_last && !aborted; cb += kMaxPassChunks) {
-            const int npass = (int)min((int64_t)kMaxPassChunks, c_last - cb + 1);
-            // ---- window prologue: bins every pixel can reach per stage ----
-            for (int q = t; q < npass; q += blockDim.x) {
-                s_wlo[q] = INT_MAX;
-                s_whi[q] = INT_MIN;
-            }
-            __syncthreads();
-            for (int q = 0; q < npass; ++q) {
-                const int64_t K = (cb + q) * kStage;
-                int blo = INT_MAX, bhi = INT_MIN;
-                if (active && lo <= K + kStage - 1 && hi >= K) {
-                    const int64_t ka = K, kb = min(K + kStage - 1, P.naz - 1);
-                    const float4 ta = __ldg(&pff[ka].hi), tb = __ldg(&pff[kb].hi);
-                    const float dev = __ldg(&sdev[cb + q]);
-                    const float ax = pf.xh - ta.x, ay = pf.yh - ta.y, az = pf.zh - ta.z;
-                    const float bx = pf.xh - tb.x, by = pf.yh - tb.y, bz = pf.zh - tb.z;
-                    const float ra = sqrtf(ax * ax + ay * ay + az * az);
-                    const float rb = sqrtf(bx * bx + by * by + bz * bz);
-                    const float sx = tb.x - ta.x, sy = tb.y - ta.y, sz = tb.z - ta.z;
-                    const float ss = sx * sx + sy * sy + sz * sz;
-                    float u = ss > 0.f ? (ax * sx + ay * sy + az * sz) / ss : 0.f;
-                    u = fminf(fmaxf(u, 0.f), 1.f);
-                    const float cx = ax - u * sx, cy = ay - u * sy, cz = az - u * sz;
-                    const float rc = sqrtf(cx * cx + cy * cy + cz * cz);
-                    const float rmin = fminf(fminf(ra, rb), rc) - dev;
-                    const float rmax = fmaxf(ra, rb) + dev;
-                    blo = (int)floorf((rmin - P.near_hi) * P.inv_dra_f) - 1;
-                    bhi = (int)ceilf((rmax - P.near_hi) * P.inv_dra_f) + 1;
-                }
-                for (int o = 16; o > 0; o >>= 1) {
-                    blo = min(blo, __shfl_xor_sync(0xffffffffu, blo, o));
-                    bhi = max(bhi, __shfl_xor_sync(0xffffffffu, bhi, o));
-                }
-                if ((t & 31) == 0 && blo <= bhi) {
-                    atomicMin(&s_wlo[q], blo);
-                    atomicMax(&s_whi[q], bhi);
-                }
-            }
-            __syncthreads();
-
-            // ---- producer: stage q of this pass into buffer s ----
-            // window start of stage q: even (16-byte aligned TMA x coordinate),
-            // inside [0, nra]; 0 for a stage no pixel of the tile reaches
-            auto window_start = [&](int q) {
-                const int wl = s_wlo[q], wh = s_whi[q];
-                if (wl > wh) return 0;
-                return (int)min((int64_t)max(wl, 0), P.nra) & ~1;
-            };
-            auto issue = [&](int q, int s, uint32_t use) {
-                unsigned char *base = smem + (size_t)s * SM::stage_bytes;
-                const int64_t K = (cb + q) * kStage;
-                mbar_arrive_expect_tx(&full_bar[s], (uint32_t)SM::stage_bytes);
-                tma_load_2d(base, raw_map, &full_bar[s], window_start(q), (int)K);
-                bulk_load(base + SM::raw_bytes, ptab + K, (uint32_t)SM::tab_bytes, &full_bar[s]);
-                pending[s] = true;
-                pending_parity[s] = use & 1;
-            };
-            if (t == 0) issue(0, it & 1, it >> 1);
-
-            for (int q = 0; q < npass; ++q, ++it) {
-                const int s = it & 1;
-                if (t == 0 && q + 1 < npass) issue(q + 1, s ^ 1, (it + 1) >> 1);
-                const int64_t c = cb + q;
-                const int64_t K = c * kStage;
-                // ---- chunk reference: once per CHUNK pulses, before the wait ----
-                const int64_t chunk = c / R;
-                if (chunk != cur_chunk) {
-                    cur_chunk = chunk;
-                    const int64_t C0 = chunk * CHUNK;
-                    gwork = active && lo <= C0 + CHUNK - 1 && hi >= C0;
-                    gre = gim = 0.f;
-                    if (gwork) {
-                        ++chunks;
-                        ChunkRef ref;
-                        ref.emax = __ldg(&ctab[chunk].emax);
-                        ref.thi = __ldg(&ctab[chunk].thi);
-                        ref.tlo = __ldg(&ctab[chunk].tlo);
-                        chunk_setup(P, pf, ref, S);
-                    } else {
-                        safe_setup(S, 0);
-                    }
-                }
-                const bool ready = mbar_wait(&full_bar[s], (it >> 1) & 1, kWaitLimit);
-                if (t == 0 && ready) pending[s] = false;
-                const int jmin = (int)(lo > K ? lo - K : 0);
-                const int jmax = (int)(hi < K + kStage - 1 ? hi - K : kStage - 1);
-                const bool work = ready && gwork && jmin <= jmax;
-                const float2 *sraw =
-                    reinterpret_cast<const float2 *>(smem + (size_t)s * SM::stage_bytes);
-                const float4 *stab = reinterpret_cast<const float4 *>(
-                    smem + (size_t)s * SM::stage_bytes + SM::raw_bytes);
-                const int b0 = window_start(q);
-                // window covers every bin the tile can reach and lies inside
-                // the kept bins 0..nra-2: no per-pulse validity/window tests
-                const bool win_ok = s_wlo[q] >= 0 && (int64_t)s_whi[q] <= P.nra - 2 &&
-                                    s_whi[q] - b0 < W;
-                const bool exact = work && S.exact;
-                const bool fast = __all_sync(0xffffffffu, !work || (jmin == 0 &&
-                                                                    jmax == kStage - 1 &&
-                                                                    win_ok && !exact));
-                if (!__any_sync(0xffffffffu, work)) {
-                    // no pixel of this warp has pulses in the stage
-                } else if (exact) {
-                    const double px = P.x[ii], py = P.y[ii], pz = P.z[ii];
-                    double sre = 0.0, sim = 0.0;
-                    for (int j = jmin; j <= jmax; ++j) {
-                        int64_t bin;
-                        double tre, tim;
-                        if (exact_term(P, px, py, pz, K + j, &bin, &tre, &tim)) {
-                            sre += tre;
-                            sim += tim;
-                            ++n;
-                            if (kChecksum) cs += mix64(K + j, bin);
-                        }
-                    }
-                    kahan_add(acc_re, cmp_re, (float)sre);
-                    kahan_add(acc_im, cmp_im, (float)sim);
-                } else {
-                    // lanes without work use their (zero or other-chunk) setup
-                    // and read column 0 or a clamped column; nothing is added
-                    const int colbias = S.n0 - b0 - 0x4B400000;
-                    const float tie = 0.5f - S.eps;
-                    float sre = gre, sim = gim;
-                    uint32_t amb_mask = 0, miss_mask = 0, valid_mask;
-                    if (fast) {
-                        valid_mask = 0xffffffffu;
-#pragma unroll
-                        for (int j = 0; j < kStage; ++j) {
-                            float D, dR;
-                            int col;
-                            bool amb;
-                            pulse_eval(S, stab[j], P.inv_dra_f, colbias, tie, D, dR, col, amb);
-                            if (amb) amb_mask |= 1u << j;
-                            col = (int)min((unsigned)col, (unsigned)(W - 1));
-                            const float2 v = sraw[j * W + col];
-                            float wc, ws;
-                            pulse_phasor(S, D, dR, P.beta_f, wc, ws);
-                            sre = fmaf(v.x, wc, fmaf(v.y, ws, sre));
-                            sim = fmaf(v.y, wc, fmaf(-v.x, ws, sim));
-                            if (kChecksum && work) cs += mix64(K + j, col + b0);
-                        }
-                    } else {
-                        valid_mask = 0;
-                        const uint32_t apmask =
-                            work ? (((jmax == 31) ? 0xffffffffu : ((1u << (jmax + 1)) - 1u)) &
-                                    ~((1u << jmin) - 1u))
-                                 : 0u;
-#pragma unroll
-                        for (int j = 0; j < kStage; ++j) {
-                            float D, dR;
-                            int col;
-                            bool amb;
-                            pulse_eval(S, stab[j], P.inv_dra_f, colbias, tie, D, dR, col, amb);
-                            const bool inap = (apmask >> j) & 1u;
-                            const int bin = col + b0;
-                            const bool ok = inap && (unsigned)bin < nra_m1;
-                            const bool inw = (unsigned)col < (unsigned)W;
-                            float2 v = make_float2(0.f, 0.f);
-                            if (ok && inw) v = sraw[j * W + col];
-                            if (ok) valid_mask |= 1u << j;
-                            if (ok && !inw) miss_mask |= 1u << j;
-                            if (inap && amb) amb_mask |= 1u << j;
-                            float wc, ws;
-                            pulse_phasor(S, D, dR, P.beta_f, wc, ws);
-                            sre = fmaf(v.x, wc, fmaf(v.y, ws, sre));
-                            sim = fmaf(v.y, wc, fmaf(-v.x, ws, sim));
-                            if (kChecksum && ok) cs += mix64(K + j, bin);
-                        }
-                    }
-                    if (work) {
-                        // rare fix-ups: ties re-derived exactly, window misses from L2
-                        uint32_t fix = amb_mask | miss_mask;
-                        const float2 *rowc = P.raw + K * P.pitch;
-                        while (fix) {
-                            const int j = __ffs(fix) - 1;
-                            fix &= fix - 1;
-                            float D, dR;
-                            int col;
-                            bool amb;
-                            pulse_eval(S, stab[j], P.inv_dra_f, colbias, tie, D, dR, col, amb);
-                            int bin_old = col + b0;
-                            bool ok_old;
-                            float2 v_old = make_float2(0.f, 0.f);
-                            if (fast) {
-                                col = (int)min((unsigned)col, (unsigned)(W - 1));
-                                bin_old = col + b0;
-                                ok_old = true;
-                                v_old = sraw[j * W + col];
-                            } else {
-                                ok_old = (unsigned)bin_old < nra_m1;
-                                if (ok_old && (unsigned)col < (unsigned)W) v_old = sraw[j * W + col];
-                            }
-                            int bin = bin_old;
-                            if ((amb_mask >> j) & 1u) {
-                                bin = resolve_bin(P, pf, ii, pff, K + j);
-                                ++ambiguous;
-                            }
-                            const bool ok_new = bin >= 0 && (unsigned)bin < nra_m1;
-                            float2 v_new = make_float2(0.f, 0.f);
-                            if (ok_new) {
-                                const int cn = bin - b0;
-                                if ((unsigned)cn < (unsigned)W) {
-                                    v_new = sraw[j * W + cn];
-                                } else {
-                                    v_new = __ldg(rowc + (j * pitch + bin));
-                                    ++misses;
-                                }
-                            }
-                            float wc, ws;
-                            pulse_phasor(S, D, dR, P.beta_f, wc, ws);
-                            const float dx = v_new.x - v_old.x, dy = v_new.y - v_old.y;
-                            sre = fmaf(dx, wc, fmaf(dy, ws, sre));
-                            sim = fmaf(dy, wc, fmaf(-dx, ws, sim));
-                            valid_mask = ok_new ? (valid_mask | (1u << j)) : (valid_mask & ~(1u << j));
-                            if (kChecksum) {
-                                if (ok_old) cs -= mix64(K + j, bin_old);
-                                if (ok_new) cs += mix64(K + j, bin);
-                            }
-                        }
-                        n += __popc(valid_mask);
-                        gre = sre;
-                        gim = sim;
-                    }
-                }
-                // end of the chunk: rotate its partial by the reference phasor
-                if (gwork && !S.exact && (c % R == R - 1 || c == c_last)) {
-                    const float rre = fmaf(gre, S.w0re, -(gim * S.w0im));
-                    const float rim = fmaf(gre, S.w0im, gim * S.w0re);
-                    kahan_add(acc_re, cmp_re, rre);
-                    kahan_add(acc_im, cmp_im, rim);
-                    gre = gim = 0.f;
-                }
-                // every thread is done with buffer s before it is refilled
-                if (__syncthreads_or(!ready)) {
-                    aborted = true;
-                    break;
-                }
-            }
-        }
-    }
-
-    st.ambiguous += ambiguous;
-    st.chunks += chunks;
-    st.misses += misses;
-    if (aborted) return false;
-    if (inside) {
-        double2 res = make_double2(0.0, 0.0);
-        if (n > 0) {
-            const double inv = 1.0 / (double)n;
-            res = make_double2(((double)acc_re - (double)cmp_re) * inv,
-                               ((double)acc_im - (double)cmp_im) * inv);
-        }
-        o.out[ii] = res;
-        if (o.nvalid) o.nvalid[ii] = n;
-        if (kChecksum) o.checksum[ii] = cs;
-    }
-    return true;
-}
-
-template <int CHUNK, int W>
-__device__ __forceinline__ StagedCta staged_cta_init(unsigned char *smem_dyn, uint64_t *full_bar,
-                                                     int *s_wlo, int *s_whi, long long *s_lo,
-                                                     long long *s_hi)
-{
-    StagedCta cta;
-    // TMA tile loads without swizzle need 128-byte aligned destinations
-    cta.smem = reinterpret_cast<unsigned char *>(
-        (reinterpret_cast<uintptr_t>(smem_dyn) + 127) & ~(uintptr_t)127);
-    cta.full_bar = full_bar;
-    cta.s_wlo = s_wlo;
-    cta.s_whi = s_whi;
-    cta.s_lo = s_lo;
-    cta.s_hi = s_hi;
-    cta.it = 0;
-    cta.pending[0] = cta.pending[1] = false;
-    cta.pending_parity[0] = cta.pending_parity[1] = 0;
-    if (threadIdx.x == 0) {
-        mbar_init(&full_bar[0], 1);
-        mbar_init(&full_bar[1], 1);
-        mbar_fence_init();
-    }
-    __syncthreads();
-    return cta;
-}
-
-// A bounded wait gave up: mark the status block and let copies still in
-// flight land before the CTA's shared memory goes away.
-__device__ __forceinline__ void staged_abort(StagedCta &cta, StatusBlock *status,
-                                             unsigned long long *counters)
-{
-    if (threadIdx.x == 0) {
-        atomicOr(&status->error, 1u);
-        atomicExch(&status->where, 1u);
-        for (int s = 0; s < 2; ++s)
-            if (cta.pending[s]) mbar_wait(&cta.full_bar[s], cta.pending_parity[s], kWaitLimit);
-        if (counters) atomicAdd(counters + SARBP_CTR_TIMEOUTS, 1ull);
-    }
-}
-
-__device__ __forceinline__ void flush_stats(TileStats &st, unsigned long long *counters)
-{
-    if (!counters) return;
-    for (int o = 16; o > 0; o >>= 1) {
-        st.ambiguous += __shfl_xor_sync(0xffffffffu, st.ambiguous, o);
-        st.chunks += __shfl_xor_sync(0xffffffffu, st.chunks, o);
-        st.misses += __shfl_xor_sync(0xffffffffu, st.misses, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        if (st.ambiguous)
-            atomicAdd(counters + SARBP_CTR_AMBIGUOUS, (unsigned long long)st.ambiguous);
-        if (st.chunks) atomicAdd(counters + SARBP_CTR_CHUNKS, (unsigned long long)st.chunks);
-        if (st.misses) atomicAdd(counters + SARBP_CTR_WINDOW_MISS, (unsigned long long)st.misses);
-    }
-}
-
-// One scene: one CTA per pixel tile.
-template <int CHUNK, int T0, int T1, int W, bool kChecksum>
-__global__ void __launch_bounds__(T0 *T1)
-focus_mixed_staged_kernel(const SceneParams P, const __grid_constant__ CUtensorMap raw_map,
-                          const TileTables tb, int64_t ntile0, const TileOutputs o,
-                          unsigned long long *__restrict__ counters, StatusBlock *status)
-{
-    extern __shared__ unsigned char smem_dyn[];
-    __shared__ __align__(8) uint64_t full_bar[2];
-    __shared__ int s_wlo[kMaxPassChunks], s_whi[kMaxPassChunks];
-    __shared__ long long s_lo, s_hi;
-    StagedCta cta = staged_cta_init<CHUNK, W>(smem_dyn, full_bar, s_wlo, s_whi, &s_lo, &s_hi);
-    TileStats st{0, 0, 0};
-    const bool ok = staged_tile<CHUNK, T0, T1, W, kChecksum>(
-        cta, P, &raw_map, tb, blockIdx.x % ntile0, blockIdx.x / ntile0, o, st);
-    if (!ok) {
-        staged_abort(cta, status, counters);
-        return;
-    }
-    flush_stats(st, counters);
-}
-
-// One scene, persistent grid: CTAs pull tiles in decreasing estimated cost
-// (the order prepared in the workspace) until the queue is empty, so the
-// longest tiles start first and no wave of CTAs ends half empty.
-template <int CHUNK, int T0, int T1, int W, bool kChecksum>
-__global__ void __launch_bounds__(T0 *T1)
-focus_mixed_staged_queue_kernel(const SceneParams P, const __grid_constant__ CUtensorMap raw_map,
-                                const TileTables tb, int64_t ntile0,
-                                const int32_t *__restrict__ order, int64_t ntiles,
-                                unsigned long long *cursor, const TileOutputs o,
-                                unsigned long long *__restrict__ counters, StatusBlock *status)
-{
-    extern __shared__ unsigned char smem_dyn[];
-    __shared__ __align__(8) uint64_t full_bar[2];
-    __shared__ int s_wlo[kMaxPassChunks], s_whi[kMaxPassChunks];
-    __shared__ long long s_lo, s_hi;
-    __shared__ long long s_item[2];
-    StagedCta cta = staged_cta_init<CHUNK, W>(smem_dyn, full_bar, s_wlo, s_whi, &s_lo, &s_hi);
-    TileStats st{0, 0, 0};
-    for (int round = 0;; ++round) {
-        if (threadIdx.x == 0) s_item[round & 1] = (long long)atomicAdd(cursor, 1ull);
-        __syncthreads();
-        const long long item = s_item[round & 1];
-        if (item >= ntiles) break;
-        const int64_t tile = order[item];
-        if (tile < 0 || tile >= ntiles) continue;   // a queue prepared for other pixels
-        const bool ok = staged_tile<CHUNK, T0, T1, W, kChecksum>(
-            cta, P, &raw_map, tb, tile % ntile0, tile / ntile0, o, st);
-        if (!ok) {
-            staged_abort(cta, status, counters);
-            return;
-        }
-    }
-    flush_stats(st, counters);
-}
-
-// Many scenes in one persistent launch: CTAs pull (scene, tile) work items
-// from a device queue (a list ordered by decreasing estimated cost and an
-// atomic cursor) until it is empty.
-template <int CHUNK, int T0, int T1, int W, bool kChecksum>
-__global__ void __launch_bounds__(T0 *T1, 3)
-focus_batch_staged_kernel(const BatchScene *__restrict__ scenes, const int2 *__restrict__ items,
-                          int64_t n_items, unsigned long long *cursor,
-                          unsigned long long *__restrict__ counters, StatusBlock *status)
-{
-    extern __shared__ unsigned char smem_dyn[];
-    __shared__ __align__(8) uint64_t full_bar[2];
-    __shared__ int s_wlo[kMaxPassChunks], s_whi[kMaxPassChunks];
-    __shared__ long long s_lo, s_hi;
-    __shared__ long long s_item[2];
-    StagedCta cta = staged_cta_init<CHUNK, W>(smem_dyn, full_bar, s_wlo, s_whi, &s_lo, &s_hi);
-    TileStats st{0, 0, 0};
-    for (int round = 0;; ++round) {
-        if (threadIdx.x == 0) s_item[round & 1] = (long long)atomicAdd(cursor, 1ull);
-        __syncthreads();
-        const long long item = s_item[round & 1];
-        if (item >= n_items) break;
-        const int2 w = items[item];
-        const BatchScene &B = scenes[w.x];
-        const int64_t tile = w.y;
-        const bool ok = staged_tile<CHUNK, T0, T1, W, kChecksum>(
-            cta, B.P, &B.map, B.tables, tile % B.ntile0, tile / B.ntile0, B.outputs, st);
-        if (!ok) {
-            staged_abort(cta, status, counters);
-            return;
-        }
-    }
-    flush_stats(st, counters);
-}
-
-// ---------------------------------------------------------------------------
-// host side
 
 static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 {
@@ -629,8 +29,8 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 }
 
 // 2-D tensor map over the pulse-major raw data: dim0 = range bins (8-byte
-// complex64 elements), dim1 = pulses; box = W bins x CHUNK pulses.
-static int make_raw_map(const SceneParams &P, int W, int rows, CUtensorMap *map)
+// complex64 elements), dim1 = pulses; box = W bins x `rows` pulses.
+int make_raw_map(const SceneParams &P, int W, int rows, CUtensorMap *map)
 {
     auto enc = tensor_map_encoder();
     if (!enc) {
@@ -657,130 +57,30 @@ static int make_raw_map(const SceneParams &P, int W, int rows, CUtensorMap *map)
     return SARBP_OK;
 }
 
-template <int CHUNK, int T0, int T1, int W>
-static int ensure_smem_attr()
-{
-    using SM = StagedSmem<CHUNK, W>;
-    // per device: the attribute belongs to the function in each context
-    static bool done[64] = {};
-    int dev = 0;
-    int rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
-    if (rc) return rc;
-    if (dev < 0 || dev >= 64 || done[dev]) return SARBP_OK;
-    const void *ks[6] = {(const void *)focus_mixed_staged_kernel<CHUNK, T0, T1, W, false>,
-                         (const void *)focus_mixed_staged_kernel<CHUNK, T0, T1, W, true>,
-                         (const void *)focus_mixed_staged_queue_kernel<CHUNK, T0, T1, W, false>,
-                         (const void *)focus_mixed_staged_queue_kernel<CHUNK, T0, T1, W, true>,
-                         (const void *)focus_batch_staged_kernel<CHUNK, T0, T1, W, false>,
-                         (const void *)focus_batch_staged_kernel<CHUNK, T0, T1, W, true>};
-    for (const void *k : ks) {
-        rc = cuda_status(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)SM::bytes),
-                         "staged smem attribute");
-        if (rc) return rc;
-    }
-    done[dev] = true;
-    return SARBP_OK;
-}
-
-static TileTables tables_of(char *ws, const MixedLayout &L)
-{
-    TileTables tb;
-    tb.ptab = reinterpret_cast<const float4 *>(ws + L.ptab);
-    tb.pff = reinterpret_cast<const PulseFF *>(ws + L.pff);
-    tb.ctab = reinterpret_cast<const ChunkRef *>(ws + L.ctab);
-    tb.sdev = reinterpret_cast<const float *>(ws + L.sdev);
-    return tb;
-}
-
-template <int CHUNK, int T0, int T1, int W>
-int launch_staged_t(const SceneParams &P, const MixedLayout &L, char *ws, bool queued,
-                    double *out, int32_t *nvalid, uint64_t *checksum, uint64_t *counters,
-                    cudaStream_t stream)
-{
-    using SM = StagedSmem<CHUNK, W>;
-    const int64_t nt0 = (P.dim0 + T0 - 1) / T0, nt1 = (P.dim1 + T1 - 1) / T1;
-    const int64_t tiles = nt0 * nt1;
-    if (tiles > 0x7fffffffLL) {
-        set_error("sarbp_focus_mixed: %lld tiles exceed the launch limit", (long long)tiles);
-        return SARBP_ERANGE;
-    }
-    CUtensorMap map;
-    int rc = make_raw_map(P, W, kStage, &map);
-    if (rc) return rc;
-    rc = ensure_smem_attr<CHUNK, T0, T1, W>();
-    if (rc) return rc;
-    const TileTables tb = tables_of(ws, L);
-    const TileOutputs o{reinterpret_cast<double2 *>(out), nvalid, checksum};
-    auto *status = reinterpret_cast<StatusBlock *>(ws + L.status);
-    auto *ctr = reinterpret_cast<unsigned long long *>(counters);
-    if (!queued) {
-        auto *k = checksum ? focus_mixed_staged_kernel<CHUNK, T0, T1, W, true>
-                           : focus_mixed_staged_kernel<CHUNK, T0, T1, W, false>;
-        k<<<(unsigned)tiles, T0 * T1, SM::bytes, stream>>>(P, map, tb, nt0, o, ctr, status);
-        return cuda_status(cudaGetLastError(), "focus_mixed_staged launch");
-    }
-    auto *k = checksum ? focus_mixed_staged_queue_kernel<CHUNK, T0, T1, W, true>
-                       : focus_mixed_staged_queue_kernel<CHUNK, T0, T1, W, false>;
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, T0 * T1, SM::bytes),
-                     "queue occupancy");
-    if (rc) return rc;
-    const int64_t grid = std::min<int64_t>(tiles, (int64_t)std::max(1, per_sm) * sms);
-    auto *cursor = reinterpret_cast<unsigned long long *>(ws + L.cursor);
-    rc = cuda_status(cudaMemsetAsync(cursor, 0, sizeof(*cursor), stream), "queue cursor reset");
-    if (rc) return rc;
-    k<<<(unsigned)grid, T0 * T1, SM::bytes, stream>>>(
-        P, map, tb, nt0, reinterpret_cast<const int32_t *>(ws + L.vals_out), tiles, cursor, o,
-        ctr, status);
-    return cuda_status(cudaGetLastError(), "focus_mixed_staged_queue launch");
-}
-
-// (chunk, tile0, tile1, window) variants the staged kernels are built for.
-#define SARBP_STAGED_TILINGS(X) \
-    X(32, 16, 16, 128) X(32, 16, 16, 160) X(32, 16, 8, 128) X(32, 32, 8, 128) X(32, 64, 4, 128) \
-    X(64, 16, 16, 128) X(64, 16, 16, 160) X(64, 16, 8, 128) X(64, 32, 8, 128) X(64, 64, 4, 128)
+// Dispatch on the chunk size; the (tile, window) variants of each chunk size
+// are built in their own translation unit.
+SARBP_STAGED_CHUNK_EXTERN(extern, 32)
+SARBP_STAGED_CHUNK_EXTERN(extern, 64)
+SARBP_STAGED_CHUNK_EXTERN(extern, 128)
 
 int launch_staged(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L, char *ws,
                   bool queued, double *out, int32_t *nvalid, uint64_t *checksum,
                   uint64_t *counters, cudaStream_t stream)
 {
-#define X(C, A, B, W)                                                                       \
-    if (T.chunk == C && T.tile0 == A && T.tile1 == B && T.window == W)                      \
-        return launch_staged_t<C, A, B, W>(P, L, ws, queued, out, nvalid, checksum, counters, \
+    switch (T.chunk) {
+        case 32:
+            return launch_staged_chunk<32>(P, T, L, ws, queued, out, nvalid, checksum, counters,
                                            stream);
-    SARBP_STAGED_TILINGS(X)
-#undef X
-    set_error("staged path: unsupported tuning chunk=%d tile=%dx%d window=%d", T.chunk, T.tile0,
-              T.tile1, T.window);
-    return SARBP_EINVAL;
-}
-
-// ---------------------------------------------------------------------------
-// batches: many scenes, one persistent launch
-
-struct BatchHeader {
-    StatusBlock status;
-    unsigned long long cursor;      // next work item
-    int32_t nscenes, key;           // scene slots, tiling key of the batch
-    int64_t max_items;
-    unsigned char pad[256 - 8 - 8 - 8];
-};
-
-struct BatchLayout {
-    size_t header, scenes, items, total;
-};
-
-static BatchLayout batch_layout(int nscenes, int64_t max_items)
-{
-    BatchLayout L{};
-    L.header = 0;
-    L.scenes = (sizeof(BatchHeader) + 255) & ~(size_t)255;
-    L.items = (L.scenes + sizeof(BatchScene) * (size_t)nscenes + 255) & ~(size_t)255;
-    L.total = (L.items + sizeof(int2) * (size_t)max_items + 255) & ~(size_t)255;
-    return L;
+        case 64:
+            return launch_staged_chunk<64>(P, T, L, ws, queued, out, nvalid, checksum, counters,
+                                           stream);
+        case 128:
+            return launch_staged_chunk<128>(P, T, L, ws, queued, out, nvalid, checksum, counters,
+                                            stream);
+        default:
+            set_error("staged path: unsupported chunk %d", T.chunk);
+            return SARBP_EINVAL;
+    }
 }
 
 int64_t batch_workspace_size(int nscenes, int64_t max_items)
@@ -803,8 +103,8 @@ int batch_set_scene(void *bws, size_t bytes, int slot, int nscenes, const SceneP
                     const sarbp_tuning &T, void *scene_ws, size_t scene_ws_bytes, double *out,
                     int32_t *nvalid, uint64_t *checksum, cudaStream_t stream)
 {
-    if (!T.staged || (T.chunk != 32 && T.chunk != 64)) {
-        set_error("batch path: needs the staged kernel with 32- or 64-pulse chunks");
+    if (!T.staged || (T.chunk != 32 && T.chunk != 64 && T.chunk != 128)) {
+        set_error("batch path: needs the staged kernel (32-, 64- or 128-pulse chunks)");
         return SARBP_EINVAL;
     }
     const BatchLayout BL = batch_layout(nscenes, 0);
@@ -847,33 +147,6 @@ int batch_set_items(void *bws, size_t bytes, int nscenes, const int32_t *items, 
                        "batch items upload");
 }
 
-template <int C, int A, int B, int W>
-static int launch_batch_t(char *bws, const BatchLayout &BL, int64_t n_items, bool diag,
-                          uint64_t *counters, cudaStream_t stream)
-{
-    using SM = StagedSmem<C, W>;
-    int rc = ensure_smem_attr<C, A, B, W>();
-    if (rc) return rc;
-    auto *k = diag ? focus_batch_staged_kernel<C, A, B, W, true>
-                   : focus_batch_staged_kernel<C, A, B, W, false>;
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, A * B, SM::bytes),
-                     "batch occupancy");
-    if (rc) return rc;
-    const int64_t grid = std::min<int64_t>(n_items, (int64_t)std::max(1, per_sm) * sms);
-    auto *hdr = reinterpret_cast<BatchHeader *>(bws);
-    rc = cuda_status(cudaMemsetAsync(&hdr->cursor, 0, sizeof(hdr->cursor), stream),
-                     "batch cursor reset");
-    if (rc) return rc;
-    k<<<(unsigned)grid, A * B, SM::bytes, stream>>>(
-        reinterpret_cast<const BatchScene *>(bws + BL.scenes),
-        reinterpret_cast<const int2 *>(bws + BL.items), n_items, &hdr->cursor,
-        reinterpret_cast<unsigned long long *>(counters), &hdr->status);
-    return cuda_status(cudaGetLastError(), "focus_batch_staged launch");
-}
-
 int batch_focus(void *bws, size_t bytes, int nscenes, const sarbp_tuning &T, int64_t n_items,
                 bool diag, uint64_t *counters, cudaStream_t stream)
 {
@@ -884,14 +157,18 @@ int batch_focus(void *bws, size_t bytes, int nscenes, const sarbp_tuning &T, int
     }
     if (n_items <= 0) return SARBP_OK;
     char *ws = static_cast<char *>(bws);
-#define X(C, A, B, W)                                                                       \
-    if (T.staged && T.chunk == C && T.tile0 == A && T.tile1 == B && T.window == W)          \
-        return launch_batch_t<C, A, B, W>(ws, BL, n_items, diag, counters, stream);
-    SARBP_STAGED_TILINGS(X)
-#undef X
-    set_error("batch path: unsupported tuning chunk=%d tile=%dx%d staged=%d", T.chunk, T.tile0,
-              T.tile1, T.staged);
-    return SARBP_EINVAL;
+    if (!T.staged) {
+        set_error("batch path: needs the staged kernel (staged > 0)");
+        return SARBP_EINVAL;
+    }
+    switch (T.chunk) {
+        case 32: return launch_batch_chunk<32>(ws, BL, T, n_items, diag, counters, stream);
+        case 64: return launch_batch_chunk<64>(ws, BL, T, n_items, diag, counters, stream);
+        case 128: return launch_batch_chunk<128>(ws, BL, T, n_items, diag, counters, stream);
+        default:
+            set_error("batch path: unsupported chunk %d", T.chunk);
+            return SARBP_EINVAL;
+    }
 }
 
 // Estimated cost of each tile of a scene: the sum of its pixels' kept

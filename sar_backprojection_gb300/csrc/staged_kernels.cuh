@@ -1,5 +1,7 @@
-// focus_staged.cu -- mixed-precision back-projection with TMA-staged raw
-// windows.
+#pragma once
+// staged_kernels.cuh -- mixed-precision back-projection with TMA-staged raw
+// windows: device code and launch templates (instantiated per chunk size in
+// staged_c32.cu, staged_c64.cu, staged_c128.cu).
 //
 // Same decomposition and precision plan as the gather kernel
 // (focus_mixed.cu, mixed_common.cuh), but each CTA stages, per 32-pulse
@@ -11,8 +13,8 @@
 // memory instead of L1/L2.
 //
 // The float-float reference (chunk_setup) is computed once per chunk of
-// CHUNK = 32 or 64 pulses (reference pulse mid-chunk, so |e| <= 16 m for
-// either), before the wait for the chunk's first stage; a chunk's stages sum
+// CHUNK = 32, 64 or 128 pulses (reference pulse mid-chunk), before the wait
+// for the chunk's first stage; a chunk's stages sum
 // into one FP32 partial that is rotated by the reference phasor and added to
 // the Kahan accumulator once per chunk.
 //
@@ -32,7 +34,6 @@
 #include <cstdio>
 #include <cstring>
 
-#include <cub/device/device_radix_sort.cuh>
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -159,6 +160,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
     const float4 *ptab = tb.ptab;
     const PulseFF *pff = tb.pff;
     const ChunkRef *ctab = tb.ctab;
+    const float *sdev = tb.sdev;
 
     const int t = threadIdx.x;
     int64_t i0, i1;
@@ -193,33 +195,44 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
     bool *pending = cta.pending;
     uint32_t *pending_parity = cta.pending_parity;
     bool aborted = false;
+    constexpr int R = CHUNK / kStage;     // stages per chunk (setup group)
+    ChunkSetup S;
+    safe_setup(S, 0);
+    bool gwork = false;                   // pixel has pulses in the current chunk
+    int64_t cur_chunk = -1;
+    float gre = 0.f, gim = 0.f;           // FP32 partial sum of the current chunk
     if (thi >= 0) {
-        const int64_t c_first = tlo / CHUNK, c_last = thi / CHUNK;
+        const int64_t c_first = tlo / kStage, c_last = thi / kStage;
         for (int64_t cb = c_first; cb <= c_last && !aborted; cb += kMaxPassChunks) {
             const int npass = (int)min((int64_t)kMaxPassChunks, c_last - cb + 1);
-            // ---- window prologue: bins every pixel can reach per chunk ----
+            // ---- window prologue: bins every pixel can reach per stage ----
             for (int q = t; q < npass; q += blockDim.x) {
                 s_wlo[q] = INT_MAX;
                 s_whi[q] = INT_MIN;
             }
             __syncthreads();
             for (int q = 0; q < npass; ++q) {
-                const int64_t K = (cb + q) * CHUNK;
+                const int64_t K = (cb + q) * kStage;
                 int blo = INT_MAX, bhi = INT_MIN;
-                if (active && lo <= K + CHUNK - 1 && hi >= K) {
-                    const int64_t ka = K, kb = min(K + CHUNK - 1, P.naz - 1);
+                if (active && lo <= K + kStage - 1 && hi >= K) {
+                    const int64_t ka = K, kb = min(K + kStage - 1, P.naz - 1);
                     const float4 ta = __ldg(&pff[ka].hi), tb = __ldg(&pff[kb].hi);
-                    const float dev = __ldg(&ctab[cb + q].thi.w);
+                    const float dev = __ldg(&sdev[cb + q]);
                     const float ax = pf.xh - ta.x, ay = pf.yh - ta.y, az = pf.zh - ta.z;
                     const float bx = pf.xh - tb.x, by = pf.yh - tb.y, bz = pf.zh - tb.z;
-                    const float ra = sqrtf(ax * ax + ay * ay + az * az);
-                    const float rb = sqrtf(bx * bx + by * by + bz * bz);
+                    // approximate square roots and quotient (relative error
+                    // ~1e-6, ~4 mm at 4 km): the window keeps a 1-bin margin
+                    const float a2 = ax * ax + ay * ay + az * az;
+                    const float b2 = bx * bx + by * by + bz * bz;
+                    const float ra = a2 > 0.f ? a2 * rsqrtf(a2) : 0.f;
+                    const float rb = b2 > 0.f ? b2 * rsqrtf(b2) : 0.f;
                     const float sx = tb.x - ta.x, sy = tb.y - ta.y, sz = tb.z - ta.z;
                     const float ss = sx * sx + sy * sy + sz * sz;
-                    float u = ss > 0.f ? (ax * sx + ay * sy + az * sz) / ss : 0.f;
+                    float u = ss > 0.f ? __fdividef(ax * sx + ay * sy + az * sz, ss) : 0.f;
                     u = fminf(fmaxf(u, 0.f), 1.f);
                     const float cx = ax - u * sx, cy = ay - u * sy, cz = az - u * sz;
-                    const float rc = sqrtf(cx * cx + cy * cy + cz * cz);
+                    const float c2 = cx * cx + cy * cy + cz * cz;
+                    const float rc = c2 > 0.f ? c2 * rsqrtf(c2) : 0.f;
                     const float rmin = fminf(fminf(ra, rb), rc) - dev;
                     const float rmax = fmaxf(ra, rb) + dev;
                     blo = (int)floorf((rmin - P.near_hi) * P.inv_dra_f) - 1;
@@ -236,9 +249,9 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
             }
             __syncthreads();
 
-            // ---- producer: stage chunk q of this pass into stage s ----
-            // window start of chunk q: even (16-byte aligned TMA x coordinate),
-            // inside [0, nra]; 0 for a chunk no pixel of the tile reaches
+            // ---- producer: stage q of this pass into buffer s ----
+            // window start of stage q: even (16-byte aligned TMA x coordinate),
+            // inside [0, nra]; 0 for a stage no pixel of the tile reaches
             auto window_start = [&](int q) {
                 const int wl = s_wlo[q], wh = s_whi[q];
                 if (wl > wh) return 0;
@@ -246,7 +259,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
             };
             auto issue = [&](int q, int s, uint32_t use) {
                 unsigned char *base = smem + (size_t)s * SM::stage_bytes;
-                const int64_t K = (cb + q) * CHUNK;
+                const int64_t K = (cb + q) * kStage;
                 mbar_arrive_expect_tx(&full_bar[s], (uint32_t)SM::stage_bytes);
                 tma_load_2d(base, raw_map, &full_bar[s], window_start(q), (int)K);
                 bulk_load(base + SM::raw_bytes, ptab + K, (uint32_t)SM::tab_bytes, &full_bar[s]);
@@ -258,13 +271,31 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
             for (int q = 0; q < npass; ++q, ++it) {
                 const int s = it & 1;
                 if (t == 0 && q + 1 < npass) issue(q + 1, s ^ 1, (it + 1) >> 1);
+                const int64_t c = cb + q;
+                const int64_t K = c * kStage;
+                // ---- chunk reference: once per CHUNK pulses, before the wait ----
+                const int64_t chunk = c / R;
+                if (chunk != cur_chunk) {
+                    cur_chunk = chunk;
+                    const int64_t C0 = chunk * CHUNK;
+                    gwork = active && lo <= C0 + CHUNK - 1 && hi >= C0;
+                    gre = gim = 0.f;
+                    if (gwork) {
+                        ++chunks;
+                        ChunkRef ref;
+                        ref.emax = __ldg(&ctab[chunk].emax);
+                        ref.thi = __ldg(&ctab[chunk].thi);
+                        ref.tlo = __ldg(&ctab[chunk].tlo);
+                        chunk_setup(P, pf, ref, S);
+                    } else {
+                        safe_setup(S, 0);
+                    }
+                }
                 const bool ready = mbar_wait(&full_bar[s], (it >> 1) & 1, kWaitLimit);
                 if (t == 0 && ready) pending[s] = false;
-                const int64_t c = cb + q;
-                const int64_t K = c * CHUNK;
                 const int jmin = (int)(lo > K ? lo - K : 0);
-                const int jmax = (int)(hi < K + CHUNK - 1 ? hi - K : CHUNK - 1);
-                const bool work = ready && active && jmin <= jmax;
+                const int jmax = (int)(hi < K + kStage - 1 ? hi - K : kStage - 1);
+                const bool work = ready && gwork && jmin <= jmax;
                 const float2 *sraw =
                     reinterpret_cast<const float2 *>(smem + (size_t)s * SM::stage_bytes);
                 const float4 *stab = reinterpret_cast<const float4 *>(
@@ -274,22 +305,12 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                 // the kept bins 0..nra-2: no per-pulse validity/window tests
                 const bool win_ok = s_wlo[q] >= 0 && (int64_t)s_whi[q] <= P.nra - 2 &&
                                     s_whi[q] - b0 < W;
-                ChunkSetup S;
-                safe_setup(S, b0);                 // lanes without work read column 0
-                if (work) {
-                    ++chunks;
-                    ChunkRef ref;
-                    ref.emax = __ldg(&ctab[c].emax);
-                    ref.thi = __ldg(&ctab[c].thi);
-                    ref.tlo = __ldg(&ctab[c].tlo);
-                    chunk_setup(P, pf, ref, S);
-                }
                 const bool exact = work && S.exact;
                 const bool fast = __all_sync(0xffffffffu, !work || (jmin == 0 &&
-                                                                    jmax == CHUNK - 1 &&
+                                                                    jmax == kStage - 1 &&
                                                                     win_ok && !exact));
                 if (!__any_sync(0xffffffffu, work)) {
-                    // no pixel of this warp has pulses in the chunk
+                    // no pixel of this warp has pulses in the stage
                 } else if (exact) {
                     const double px = P.x[ii], py = P.y[ii], pz = P.z[ii];
                     double sre = 0.0, sim = 0.0;
@@ -306,14 +327,16 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                     kahan_add(acc_re, cmp_re, (float)sre);
                     kahan_add(acc_im, cmp_im, (float)sim);
                 } else {
+                    // lanes without work use their (zero or other-chunk) setup
+                    // and read column 0 or a clamped column; nothing is added
                     const int colbias = S.n0 - b0 - 0x4B400000;
                     const float tie = 0.5f - S.eps;
-                    float sre = 0.f, sim = 0.f;
+                    float sre = gre, sim = gim;
                     uint32_t amb_mask = 0, miss_mask = 0, valid_mask;
                     if (fast) {
                         valid_mask = 0xffffffffu;
 #pragma unroll
-                        for (int j = 0; j < CHUNK; ++j) {
+                        for (int j = 0; j < kStage; ++j) {
                             float D, dR;
                             int col;
                             bool amb;
@@ -334,7 +357,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                                     ~((1u << jmin) - 1u))
                                  : 0u;
 #pragma unroll
-                        for (int j = 0; j < CHUNK; ++j) {
+                        for (int j = 0; j < kStage; ++j) {
                             float D, dR;
                             int col;
                             bool amb;
@@ -406,13 +429,19 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                             }
                         }
                         n += __popc(valid_mask);
-                        const float rre = fmaf(sre, S.w0re, -(sim * S.w0im));
-                        const float rim = fmaf(sre, S.w0im, sim * S.w0re);
-                        kahan_add(acc_re, cmp_re, rre);
-                        kahan_add(acc_im, cmp_im, rim);
+                        gre = sre;
+                        gim = sim;
                     }
                 }
-                // every thread is done with stage s before it is refilled
+                // end of the chunk: rotate its partial by the reference phasor
+                if (gwork && !S.exact && (c % R == R - 1 || c == c_last)) {
+                    const float rre = fmaf(gre, S.w0re, -(gim * S.w0im));
+                    const float rim = fmaf(gre, S.w0im, gim * S.w0re);
+                    kahan_add(acc_re, cmp_re, rre);
+                    kahan_add(acc_im, cmp_im, rim);
+                    gre = gim = 0.f;
+                }
+                // every thread is done with buffer s before it is refilled
                 if (__syncthreads_or(!ready)) {
                     aborted = true;
                     break;
@@ -586,53 +615,32 @@ focus_batch_staged_kernel(const BatchScene *__restrict__ scenes, const int2 *__r
     flush_stats(st, counters);
 }
 
-// ---------------------------------------------------------------------------
-// host side
+// Batch workspace: header, scene records, work items.
+struct BatchHeader {
+    StatusBlock status;
+    unsigned long long cursor;      // next work item
+    int32_t nscenes, key;           // scene slots, tiling key of the batch
+    int64_t max_items;
+    unsigned char pad[256 - 8 - 8 - 8];
+};
 
-static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+struct BatchLayout {
+    size_t header, scenes, items, total;
+};
+
+inline BatchLayout batch_layout(int nscenes, int64_t max_items)
 {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
-                                             cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }
-    return fn;
+    BatchLayout L{};
+    L.header = 0;
+    L.scenes = (sizeof(BatchHeader) + 255) & ~(size_t)255;
+    L.items = (L.scenes + sizeof(BatchScene) * (size_t)nscenes + 255) & ~(size_t)255;
+    L.total = (L.items + sizeof(int2) * (size_t)max_items + 255) & ~(size_t)255;
+    return L;
 }
 
-// 2-D tensor map over the pulse-major raw data: dim0 = range bins (8-byte
-// complex64 elements), dim1 = pulses; box = W bins x CHUNK pulses.
-static int make_raw_map(const SceneParams &P, int W, int chunk, CUtensorMap *map)
-{
-    auto enc = tensor_map_encoder();
-    if (!enc) {
-        set_error("staged path: cuTensorMapEncodeTiled is unavailable");
-        return SARBP_ECUDA;
-    }
-    if ((reinterpret_cast<uintptr_t>(P.raw) & 15) || (P.pitch & 1)) {
-        set_error("staged path needs 16-byte aligned raw data rows (raw 16-byte aligned, "
-                  "raw_pitch even); got raw=%p pitch=%lld",
-                  (const void *)P.raw, (long long)P.pitch);
-        return SARBP_EINVAL;
-    }
-    cuuint64_t dims[2] = {(cuuint64_t)P.nra, (cuuint64_t)P.naz};
-    cuuint64_t strides[1] = {(cuuint64_t)P.pitch * 8};
-    cuuint32_t box[2] = {(cuuint32_t)W, (cuuint32_t)chunk};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<float2 *>(P.raw), dims,
-                     strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) {
-        set_error("staged path: cuTensorMapEncodeTiled failed (%d)", (int)r);
-        return SARBP_ECUDA;
-    }
-    return SARBP_OK;
-}
+
+// 2-D tensor map over the pulse-major raw data (focus_staged.cu).
+int make_raw_map(const SceneParams &P, int W, int rows, CUtensorMap *map);
 
 template <int CHUNK, int T0, int T1, int W>
 static int ensure_smem_attr()
@@ -660,7 +668,7 @@ static int ensure_smem_attr()
     return SARBP_OK;
 }
 
-static TileTables tables_of(char *ws, const MixedLayout &L)
+inline TileTables tables_of(char *ws, const MixedLayout &L)
 {
     TileTables tb;
     tb.ptab = reinterpret_cast<const float4 *>(ws + L.ptab);
@@ -683,7 +691,7 @@ int launch_staged_t(const SceneParams &P, const MixedLayout &L, char *ws, bool q
         return SARBP_ERANGE;
     }
     CUtensorMap map;
-    int rc = make_raw_map(P, W, CHUNK, &map);
+    int rc = make_raw_map(P, W, kStage, &map);
     if (rc) return rc;
     rc = ensure_smem_attr<CHUNK, T0, T1, W>();
     if (rc) return rc;
@@ -715,116 +723,8 @@ int launch_staged_t(const SceneParams &P, const MixedLayout &L, char *ws, bool q
     return cuda_status(cudaGetLastError(), "focus_mixed_staged_queue launch");
 }
 
-// (chunk, tile0, tile1, window) variants the staged kernels are built for.
-#define SARBP_STAGED_TILINGS(X) \
-    X(32, 16, 16, 128) X(32, 16, 16, 160) X(32, 16, 8, 128) X(32, 32, 8, 128) X(32, 64, 4, 128)
-
-int launch_staged(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L, char *ws,
-                  bool queued, double *out, int32_t *nvalid, uint64_t *checksum,
-                  uint64_t *counters, cudaStream_t stream)
-{
-#define X(C, A, B, W)                                                                       \
-    if (T.chunk == C && T.tile0 == A && T.tile1 == B && T.window == W)                      \
-        return launch_staged_t<C, A, B, W>(P, L, ws, queued, out, nvalid, checksum, counters, \
-                                           stream);
-    SARBP_STAGED_TILINGS(X)
-#undef X
-    set_error("staged path: unsupported tuning chunk=%d tile=%dx%d window=%d", T.chunk, T.tile0,
-              T.tile1, T.window);
-    return SARBP_EINVAL;
-}
-
-// ---------------------------------------------------------------------------
-// batches: many scenes, one persistent launch
-
-struct BatchHeader {
-    StatusBlock status;
-    unsigned long long cursor;      // next work item
-    int32_t nscenes, key;           // scene slots, tiling key of the batch
-    int64_t max_items;
-    unsigned char pad[256 - 8 - 8 - 8];
-};
-
-struct BatchLayout {
-    size_t header, scenes, items, total;
-};
-
-static BatchLayout batch_layout(int nscenes, int64_t max_items)
-{
-    BatchLayout L{};
-    L.header = 0;
-    L.scenes = (sizeof(BatchHeader) + 255) & ~(size_t)255;
-    L.items = (L.scenes + sizeof(BatchScene) * (size_t)nscenes + 255) & ~(size_t)255;
-    L.total = (L.items + sizeof(int2) * (size_t)max_items + 255) & ~(size_t)255;
-    return L;
-}
-
-int64_t batch_workspace_size(int nscenes, int64_t max_items)
-{
-    return (int64_t)batch_layout(nscenes, max_items).total;
-}
-
-static int tiling_tiles(const SceneParams &P, const sarbp_tuning &T, int64_t *nt0, int64_t *nt)
-{
-    if (T.tile0 <= 0 || T.tile1 <= 0) {
-        set_error("tiling: tile extents must be positive");
-        return SARBP_EINVAL;
-    }
-    *nt0 = (P.dim0 + T.tile0 - 1) / T.tile0;
-    *nt = *nt0 * ((P.dim1 + T.tile1 - 1) / T.tile1);
-    return SARBP_OK;
-}
-
-int batch_set_scene(void *bws, size_t bytes, int slot, int nscenes, const SceneParams &P,
-                    const sarbp_tuning &T, void *scene_ws, size_t scene_ws_bytes, double *out,
-                    int32_t *nvalid, uint64_t *checksum, cudaStream_t stream)
-{
-    if (!T.staged || T.chunk != 32) {
-        set_error("batch path: needs the staged kernel with 32-pulse chunks");
-        return SARBP_EINVAL;
-    }
-    const BatchLayout BL = batch_layout(nscenes, 0);
-    if (!bws || slot < 0 || slot >= nscenes || bytes < BL.items) {
-        set_error("batch path: slot %d outside the %d-scene workspace", slot, nscenes);
-        return SARBP_EINVAL;
-    }
-    const MixedLayout L = mixed_layout(P, T);
-    if (!scene_ws || scene_ws_bytes < L.base || !out) {
-        set_error("batch path: scene workspace (%zu < %zu bytes) or output missing",
-                  scene_ws_bytes, L.base);
-        return SARBP_EWORKSPACE;
-    }
-    BatchScene B;
-    memset(&B, 0, sizeof(B));
-    int rc = make_raw_map(P, T.window, T.chunk, &B.map);
-    if (rc) return rc;
-    B.P = P;
-    B.tables = tables_of(static_cast<char *>(scene_ws), L);
-    B.outputs = TileOutputs{reinterpret_cast<double2 *>(out), nvalid, checksum};
-    rc = tiling_tiles(P, T, &B.ntile0, &B.ntiles);
-    if (rc) return rc;
-    char *dst = static_cast<char *>(bws) + BL.scenes + sizeof(BatchScene) * (size_t)slot;
-    return cuda_status(cudaMemcpyAsync(dst, &B, sizeof(B), cudaMemcpyHostToDevice, stream),
-                       "batch scene upload");
-}
-
-int batch_set_items(void *bws, size_t bytes, int nscenes, const int32_t *items, int64_t n,
-                    cudaStream_t stream)
-{
-    const BatchLayout BL = batch_layout(nscenes, n);
-    if (!bws || bytes < BL.total || (n > 0 && !items)) {
-        set_error("batch path: workspace of %zu bytes too small for %lld items", bytes,
-                  (long long)n);
-        return SARBP_EWORKSPACE;
-    }
-    if (n == 0) return SARBP_OK;
-    return cuda_status(cudaMemcpyAsync(static_cast<char *>(bws) + BL.items, items,
-                                       sizeof(int2) * (size_t)n, cudaMemcpyHostToDevice, stream),
-                       "batch items upload");
-}
-
 template <int C, int A, int B, int W>
-static int launch_batch_t(char *bws, const BatchLayout &BL, int64_t n_items, bool diag,
+int launch_batch_t(char *bws, const BatchLayout &BL, int64_t n_items, bool diag,
                           uint64_t *counters, cudaStream_t stream)
 {
     using SM = StagedSmem<C, W>;
@@ -850,136 +750,49 @@ static int launch_batch_t(char *bws, const BatchLayout &BL, int64_t n_items, boo
     return cuda_status(cudaGetLastError(), "focus_batch_staged launch");
 }
 
-int batch_focus(void *bws, size_t bytes, int nscenes, const sarbp_tuning &T, int64_t n_items,
-                bool diag, uint64_t *counters, cudaStream_t stream)
+
+
+// Per-chunk-size dispatch over the (tile, window) variants; instantiated in
+// staged_c32.cu / staged_c64.cu / staged_c128.cu.  SARBP_EINVAL (with a
+// message) for a variant that is not built.
+#define SARBP_STAGED_TILES(X, C) \
+    X(C, 16, 16, 128) X(C, 16, 16, 160) X(C, 16, 8, 128) X(C, 32, 8, 128) X(C, 64, 4, 128)
+
+template <int C>
+int launch_staged_chunk(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L,
+                        char *ws, bool queued, double *out, int32_t *nvalid, uint64_t *checksum,
+                        uint64_t *counters, cudaStream_t stream)
 {
-    const BatchLayout BL = batch_layout(nscenes, n_items);
-    if (!bws || bytes < BL.total) {
-        set_error("batch path: workspace of %zu bytes too small (%zu)", bytes, BL.total);
-        return SARBP_EWORKSPACE;
-    }
-    if (n_items <= 0) return SARBP_OK;
-    char *ws = static_cast<char *>(bws);
-#define X(C, A, B, W)                                                                       \
-    if (T.staged && T.chunk == C && T.tile0 == A && T.tile1 == B && T.window == W)          \
-        return launch_batch_t<C, A, B, W>(ws, BL, n_items, diag, counters, stream);
-    SARBP_STAGED_TILINGS(X)
+#define X(C_, A, B, W)                                                                      \
+    if (T.tile0 == A && T.tile1 == B && T.window == W)                                      \
+        return launch_staged_t<C_, A, B, W>(P, L, ws, queued, out, nvalid, checksum,        \
+                                            counters, stream);
+    SARBP_STAGED_TILES(X, C)
 #undef X
-    set_error("batch path: unsupported tuning chunk=%d tile=%dx%d staged=%d", T.chunk, T.tile0,
-              T.tile1, T.staged);
+    set_error("staged path: unsupported tuning chunk=%d tile=%dx%d window=%d", T.chunk, T.tile0,
+              T.tile1, T.window);
     return SARBP_EINVAL;
 }
 
-// Estimated cost of each tile of a scene: the sum of its pixels' kept
-// aperture lengths (nominal pixel-pulses), for ordering batch work.
-template <int T0, int T1>
-__global__ void tile_cost_kernel(const SceneParams P, int64_t ntile0, int64_t ntiles,
-                                 int64_t *__restrict__ costs)
+template <int C>
+int launch_batch_chunk(char *bws, const BatchLayout &BL, const sarbp_tuning &T, int64_t n_items,
+                       bool diag, uint64_t *counters, cudaStream_t stream)
 {
-    const int64_t tile = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tile >= ntiles) return;
-    const int64_t t0 = tile % ntile0, t1 = tile / ntile0;
-    int64_t c = 0;
-    for (int b = 0; b < T1; ++b)
-        for (int a = 0; a < T0; ++a) {
-            const int64_t i0 = t0 * T0 + a, i1 = t1 * T1 + b;
-            if (i0 >= P.dim0 || i1 >= P.dim1) continue;
-            const int64_t ii = i0 + P.dim0 * i1;
-            int64_t lo, hi;
-            if (pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi))
-                c += hi - lo + 1;
-        }
-    costs[tile] = c;
-}
-
-int tile_costs(const SceneParams &P, const sarbp_tuning &T, int64_t *costs, cudaStream_t stream)
-{
-    int64_t nt0, nt;
-    int rc = tiling_tiles(P, T, &nt0, &nt);
-    if (rc) return rc;
-    const unsigned blocks = (unsigned)((nt + 127) / 128);
-#define X(A, B)                                                                             \
-    if (T.tile0 == A && T.tile1 == B) {                                                     \
-        tile_cost_kernel<A, B><<<blocks, 128, 0, stream>>>(P, nt0, nt, costs);              \
-        return cuda_status(cudaGetLastError(), "tile_cost launch");                         \
-    }
-    X(16, 16) X(16, 8) X(32, 8) X(64, 4)
+#define X(C_, A, B, W)                                                                      \
+    if (T.tile0 == A && T.tile1 == B && T.window == W)                                      \
+        return launch_batch_t<C_, A, B, W>(bws, BL, n_items, diag, counters, stream);
+    SARBP_STAGED_TILES(X, C)
 #undef X
-    set_error("tile costs: unsupported tile %dx%d", T.tile0, T.tile1);
+    set_error("batch path: unsupported tuning chunk=%d tile=%dx%d window=%d", T.chunk, T.tile0,
+              T.tile1, T.window);
     return SARBP_EINVAL;
 }
 
-template <int T0, int T1>
-__global__ void tile_key_kernel(const SceneParams P, int64_t ntile0, int64_t ntiles,
-                                uint32_t *__restrict__ keys, int32_t *__restrict__ ids)
-{
-    const int64_t tile = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tile >= ntiles) return;
-    const int64_t t0 = tile % ntile0, t1 = tile / ntile0;
-    uint64_t c = 0;
-    for (int b = 0; b < T1; ++b)
-        for (int a = 0; a < T0; ++a) {
-            const int64_t i0 = t0 * T0 + a, i1 = t1 * T1 + b;
-            if (i0 >= P.dim0 || i1 >= P.dim1) continue;
-            const int64_t ii = i0 + P.dim0 * i1;
-            int64_t lo, hi;
-            if (pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi))
-                c += (uint64_t)(hi - lo + 1);
-        }
-    keys[tile] = c > 0xffffffffull ? 0xffffffffu : (uint32_t)c;
-    ids[tile] = (int32_t)tile;
-}
-
-size_t tile_sort_bytes(int64_t ntiles)
-{
-    size_t b = 0;
-    cub::DeviceRadixSort::SortPairsDescending((void *)nullptr, b, (const uint32_t *)nullptr,
-                                              (uint32_t *)nullptr, (const int32_t *)nullptr,
-                                              (int32_t *)nullptr, (int)ntiles);
-    return b;
-}
-
-// Tiles in decreasing estimated cost (their pixels' kept aperture lengths)
-// into the workspace queue: key kernel + device radix sort, stream-ordered.
-int tile_order(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L, char *ws,
-               cudaStream_t stream)
-{
-    const int64_t nt = L.ntiles;
-    if (nt <= 0) return SARBP_OK;
-    if (nt > 0x7fffffffLL) {
-        set_error("tile order: %lld tiles exceed the queue limit", (long long)nt);
-        return SARBP_ERANGE;
-    }
-    const int64_t nt0 = (P.dim0 + T.tile0 - 1) / T.tile0;
-    auto *keys_in = reinterpret_cast<uint32_t *>(ws + L.keys_in);
-    auto *vals_in = reinterpret_cast<int32_t *>(ws + L.vals_in);
-    const unsigned blocks = (unsigned)((nt + 127) / 128);
-    bool launched = false;
-#define X(A, B)                                                                             \
-    if (!launched && T.tile0 == A && T.tile1 == B) {                                        \
-        tile_key_kernel<A, B><<<blocks, 128, 0, stream>>>(P, nt0, nt, keys_in, vals_in);    \
-        launched = true;                                                                    \
-    }
-    X(16, 16) X(16, 8) X(32, 8) X(64, 4)
-#undef X
-    if (!launched) {
-        set_error("tile order: unsupported tile %dx%d", T.tile0, T.tile1);
-        return SARBP_EINVAL;
-    }
-    int rc = cuda_status(cudaGetLastError(), "tile_key launch");
-    if (rc) return rc;
-    size_t tmp = L.sort_tmp_bytes;
-    return cuda_status(cub::DeviceRadixSort::SortPairsDescending(
-                           ws + L.sort_tmp, tmp, keys_in,
-                           reinterpret_cast<uint32_t *>(ws + L.keys_out), vals_in,
-                           reinterpret_cast<int32_t *>(ws + L.vals_out), (int)nt, 0, 32, stream),
-                       "tile order sort");
-}
-
-int tile_count(const SceneParams &P, const sarbp_tuning &T, int64_t *nt)
-{
-    int64_t nt0;
-    return tiling_tiles(P, T, &nt0, nt);
-}
+#define SARBP_STAGED_CHUNK_EXTERN(EXT, C)                                                   \
+    EXT template int launch_staged_chunk<C>(const SceneParams &, const sarbp_tuning &,      \
+                                            const MixedLayout &, char *, bool, double *,    \
+                                            int32_t *, uint64_t *, uint64_t *, cudaStream_t); \
+    EXT template int launch_batch_chunk<C>(char *, const BatchLayout &, const sarbp_tuning &, \
+                                           int64_t, bool, uint64_t *, cudaStream_t);
 
 }  // namespace sarbp
