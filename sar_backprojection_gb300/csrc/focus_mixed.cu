@@ -59,10 +59,28 @@ __host__ __device__ __forceinline__ int64_t chunk_ref(int64_t c, int chunk, int6
     return k0 < naz - 1 ? k0 : naz - 1;
 }
 
+// e of pulse k into the per-pulse table.  AoS: one float4 (x, y, z, |e|^2)
+// per pulse.  Paired (staged kernels): pulses 2p, 2p+1 share two float4,
+// (x0, x1, y0, y1) and (z0, z1, w0, w1), the operands of packed f32x2 math;
+// a 32-pulse stage still occupies float4 [K, K+32).
+__device__ __forceinline__ void store_e(float4 *ptab, int64_t k, float4 e, bool paired)
+{
+    if (!paired) {
+        ptab[k] = e;
+        return;
+    }
+    float *f = reinterpret_cast<float *>(ptab) + (k >> 1) * 8 + (k & 1);
+    f[0] = e.x;
+    f[2] = e.y;
+    f[4] = e.z;
+    f[6] = e.w;
+}
+
 // Per-pulse tables and per-chunk references; one warp per chunk.
-__global__ void chunk_table_kernel(const SceneParams P, int chunk, float4 *__restrict__ ptab,
-                                   PulseFF *__restrict__ pff, ChunkRef *__restrict__ ctab,
-                                   float *__restrict__ sdev, int64_t nchunks)
+__global__ void chunk_table_kernel(const SceneParams P, int chunk, int paired,
+                                   float4 *__restrict__ ptab, PulseFF *__restrict__ pff,
+                                   ChunkRef *__restrict__ ctab, float *__restrict__ sdev,
+                                   int64_t nchunks)
 {
     const int64_t c = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     const int lane = threadIdx.x & 31;
@@ -75,14 +93,14 @@ __global__ void chunk_table_kernel(const SceneParams P, int chunk, float4 *__res
         if (k >= P.naz) {
             // padding past the last pulse: copied with whole chunks by the
             // staged kernel, must hold finite values (never a kept pulse)
-            ptab[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            store_e(ptab, k, make_float4(0.f, 0.f, 0.f, 0.f), paired);
             continue;
         }
         const double tx = P.tx[k], ty = P.ty[k], tz = P.tz[k];
         const double ex = tx - x0, ey = ty - y0, ez = tz - z0;
         const double e2 = ex * ex + ey * ey + ez * ez;
         const float4 e = make_float4((float)ex, (float)ey, (float)ez, (float)e2);
-        ptab[k] = e;
+        store_e(ptab, k, e, paired);
         PulseFF f;
         split_ff(tx, f.hi.x, f.lo.x);
         split_ff(ty, f.hi.y, f.lo.y);
@@ -319,14 +337,14 @@ int launch_staged(const SceneParams &P, const sarbp_tuning &T, const MixedLayout
                   bool queued, double *out, int32_t *nvalid, uint64_t *checksum,
                   uint64_t *counters, cudaStream_t stream);
 
-int launch_chunk_table(const SceneParams &P, int chunk, char *ws, const MixedLayout &L,
-                       cudaStream_t stream)
+int launch_chunk_table(const SceneParams &P, int chunk, bool paired, char *ws,
+                       const MixedLayout &L, cudaStream_t stream)
 {
     const int64_t nchunks = (P.naz + chunk - 1) / chunk;
     const int warps = 8;
     const int64_t blocks = (nchunks + warps - 1) / warps;
     chunk_table_kernel<<<(unsigned)blocks, warps * 32, 0, stream>>>(
-        P, chunk, reinterpret_cast<float4 *>(ws + L.ptab), reinterpret_cast<PulseFF *>(ws + L.pff),
+        P, chunk, paired ? 1 : 0, reinterpret_cast<float4 *>(ws + L.ptab), reinterpret_cast<PulseFF *>(ws + L.pff),
         reinterpret_cast<ChunkRef *>(ws + L.ctab), reinterpret_cast<float *>(ws + L.sdev), nchunks);
     return cuda_status(cudaGetLastError(), "chunk_table launch");
 }
@@ -348,7 +366,8 @@ int launch_mixed_prepare(const SceneParams &P, const sarbp_tuning &T, void *work
     int rc = check_workspace(L, workspace, ws_bytes);
     if (rc) return rc;
     char *ws = static_cast<char *>(workspace);
-    rc = launch_chunk_table(P, T.chunk, ws, L, stream);
+    // the staged kernels read the pair-interleaved table (f32x2 operands)
+    rc = launch_chunk_table(P, T.chunk, T.staged != 0, ws, L, stream);
     if (rc) return rc;
     // persistent staged path: tiles in decreasing estimated cost
     if (T.staged == 2) return tile_order(P, T, L, ws, stream);

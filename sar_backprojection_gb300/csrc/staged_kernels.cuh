@@ -37,6 +37,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include "f32x2.cuh"
 #include "mixed_common.cuh"
 #include "tma.cuh"
 
@@ -77,6 +78,13 @@ __device__ __forceinline__ void pulse_eval(const ChunkSetup &S, float4 e, float 
     const float t = __fadd_rn(g, 12582912.0f);
     col = __float_as_int(t) + colbias;
     amb = fabsf(__fsub_rn(g, __fsub_rn(t, 12582912.0f))) > tie;
+}
+
+// e of pulse j of a stage from the pair-interleaved per-pulse table.
+__device__ __forceinline__ float4 stage_e(const float4 *stab, int j)
+{
+    const float *f = reinterpret_cast<const float *>(stab) + (j >> 1) * 8 + (j & 1);
+    return make_float4(f[0], f[2], f[4], f[6]);
 }
 
 // R^2 * exp(-j*dphi) as (wc, ws): term = (vx + j*vy) * (wc - j*ws).
@@ -334,21 +342,66 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                     float sre = gre, sim = gim;
                     uint32_t amb_mask = 0, miss_mask = 0, valid_mask;
                     if (fast) {
+                        // two pulses per f32x2 instruction, the scalar path's
+                        // operation sequence per pulse (bit-identical values)
                         valid_mask = 0xffffffffu;
+                        const f2_t mx2 = f2_dup(S.mx), my2 = f2_dup(S.my), mz2 = f2_dup(S.mz);
+                        const f2_t c1_2 = f2_dup(S.c1), c2_2 = f2_dup(S.c2), c3_2 = f2_dup(S.c3);
+                        const f2_t g0_2 = f2_dup(S.g0), a_2 = f2_dup(S.a), r0sq2 = f2_dup(S.r0sq);
+                        const f2_t idra2 = f2_dup(P.inv_dra_f), beta2 = f2_dup(P.beta_f);
+                        const f2_t magic2 = f2_dup(12582912.0f);
+                        const ulonglong2 *sp = reinterpret_cast<const ulonglong2 *>(stab);
+                        float rmax = 0.f;     // largest |g - rint(g)|: a tie test per stage
 #pragma unroll
-                        for (int j = 0; j < kStage; ++j) {
-                            float D, dR;
-                            int col;
-                            bool amb;
-                            pulse_eval(S, stab[j], P.inv_dra_f, colbias, tie, D, dR, col, amb);
-                            if (amb) amb_mask |= 1u << j;
-                            col = (int)min((unsigned)col, (unsigned)(W - 1));
-                            const float2 v = sraw[j * W + col];
-                            float wc, ws;
-                            pulse_phasor(S, D, dR, P.beta_f, wc, ws);
-                            sre = fmaf(v.x, wc, fmaf(v.y, ws, sre));
-                            sim = fmaf(v.y, wc, fmaf(-v.x, ws, sim));
-                            if (kChecksum && work) cs += mix64(K + j, col + b0);
+                        for (int p = 0; p < kStage / 2; ++p) {
+                            const ulonglong2 exy = sp[2 * p], ezw = sp[2 * p + 1];
+                            f2_t D2 = f2_fma(mz2, ezw.x, ezw.y);
+                            D2 = f2_fma(my2, exy.y, D2);
+                            D2 = f2_fma(mx2, exy.x, D2);
+                            f2_t q2 = f2_fma(c3_2, D2, c2_2);
+                            q2 = f2_fma(q2, D2, c1_2);
+                            const f2_t dR2 = f2_mul(D2, q2);
+                            const f2_t g2 = f2_fma(dR2, idra2, g0_2);
+                            const f2_t t2 = f2_add(g2, magic2);
+                            const f2_t r2 = f2_sub(g2, f2_sub(t2, magic2));
+                            float t0, t1, r0, r1;
+                            f2_unpack(t2, t0, t1);
+                            f2_unpack(r2, r0, r1);
+                            rmax = fmaxf(rmax, fmaxf(fabsf(r0), fabsf(r1)));
+                            const int col0 =
+                                (int)min((unsigned)(__float_as_int(t0) + colbias), (unsigned)(W - 1));
+                            const int col1 =
+                                (int)min((unsigned)(__float_as_int(t1) + colbias), (unsigned)(W - 1));
+                            const float2 v0 = sraw[(2 * p) * W + col0];
+                            const float2 v1 = sraw[(2 * p + 1) * W + col1];
+                            const f2_t ph2 = f2_mul(dR2, f2_fma(beta2, dR2, a_2));
+                            float ph0, ph1, s0, c0, s1, c1;
+                            f2_unpack(ph2, ph0, ph1);
+                            __sincosf(ph0, &s0, &c0);
+                            __sincosf(ph1, &s1, &c1);
+                            const f2_t w2 = f2_add(r0sq2, D2);
+                            float wc0, wc1, ws0, ws1;
+                            f2_unpack(f2_mul(w2, f2_pack(c0, c1)), wc0, wc1);
+                            f2_unpack(f2_mul(w2, f2_pack(s0, s1)), ws0, ws1);
+                            sre = fmaf(v0.x, wc0, fmaf(v0.y, ws0, sre));
+                            sim = fmaf(v0.y, wc0, fmaf(-v0.x, ws0, sim));
+                            sre = fmaf(v1.x, wc1, fmaf(v1.y, ws1, sre));
+                            sim = fmaf(v1.y, wc1, fmaf(-v1.x, ws1, sim));
+                            if (kChecksum && work) {
+                                cs += mix64(K + 2 * p, col0 + b0);
+                                cs += mix64(K + 2 * p + 1, col1 + b0);
+                            }
+                        }
+                        if (work && rmax > tie) {
+                            // a pulse near a .5 tie (rare): find which
+                            for (int j = 0; j < kStage; ++j) {
+                                float D, dR;
+                                int col;
+                                bool amb;
+                                pulse_eval(S, stage_e(stab, j), P.inv_dra_f, colbias, tie, D, dR,
+                                           col, amb);
+                                if (amb) amb_mask |= 1u << j;
+                            }
                         }
                     } else {
                         valid_mask = 0;
@@ -361,7 +414,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                             float D, dR;
                             int col;
                             bool amb;
-                            pulse_eval(S, stab[j], P.inv_dra_f, colbias, tie, D, dR, col, amb);
+                            pulse_eval(S, stage_e(stab, j), P.inv_dra_f, colbias, tie, D, dR, col, amb);
                             const bool inap = (apmask >> j) & 1u;
                             const int bin = col + b0;
                             const bool ok = inap && (unsigned)bin < nra_m1;
@@ -388,7 +441,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                             float D, dR;
                             int col;
                             bool amb;
-                            pulse_eval(S, stab[j], P.inv_dra_f, colbias, tie, D, dR, col, amb);
+                            pulse_eval(S, stage_e(stab, j), P.inv_dra_f, colbias, tie, D, dR, col, amb);
                             int bin_old = col + b0;
                             bool ok_old;
                             float2 v_old = make_float2(0.f, 0.f);
@@ -584,8 +637,16 @@ focus_mixed_staged_queue_kernel(const SceneParams P, const __grid_constant__ CUt
 // Many scenes in one persistent launch: CTAs pull (scene, tile) work items
 // from a device queue (a list ordered by decreasing estimated cost and an
 // atomic cursor) until it is empty.
+// CTAs per SM the shared memory of a (CHUNK, W) variant allows (2 or 3),
+// the register budget the batch kernel is compiled for.
+template <int CHUNK, int W>
+constexpr int staged_min_blocks()
+{
+    return StagedSmem<CHUNK, W>::bytes * 3 + 3 * 1024 <= 227 * 1024 ? 3 : 2;
+}
+
 template <int CHUNK, int T0, int T1, int W, bool kChecksum>
-__global__ void __launch_bounds__(T0 *T1, 3)
+__global__ void __launch_bounds__(T0 *T1, (staged_min_blocks<CHUNK, W>()))
 focus_batch_staged_kernel(const BatchScene *__restrict__ scenes, const int2 *__restrict__ items,
                           int64_t n_items, unsigned long long *cursor,
                           unsigned long long *__restrict__ counters, StatusBlock *status)
