@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tuning", type=str, default="",
-                    help="chunk,tile0,tile1[,staged[,window]] of the mixed kernel")
+                    help="chunk,tile0,tile1[,staged[,window[,stage]]] of the mixed kernel")
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--batch-scenes", type=int, default=48,
                     help="uneven scenes focused in one persistent graph-captured launch "
@@ -390,7 +390,7 @@ def run_ours(args, dist: Dist):
     tuning = resolve_tuning(None)
     if args.tuning:
         vals = [int(v) for v in args.tuning.split(",")]
-        for k, v in zip(("chunk", "tile0", "tile1", "staged", "window"), vals):
+        for k, v in zip(("chunk", "tile0", "tile1", "staged", "window", "stage"), vals):
             setattr(tuning, k, v)
 
     spec, workload_name = workload_spec(args, dist.rank)

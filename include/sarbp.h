@@ -74,10 +74,11 @@ typedef struct sarbp_scene {
  * Tuning of the mixed-precision kernel.  An all-zero struct (or NULL) selects
  * the library default; sarbp_default_tuning() fills the defaults explicitly.
  * Supported: staged=0 with chunk 32/64 and tiles 32x8, 64x4, 16x16; staged=1
- * or 2 with chunk 32, 64 or 128 and (tile, window) 16x16/128, 16x16/160,
- * 16x8/128, 32x8/128, 64x4/128.  The staged kernels copy raw data in
- * 32-pulse stages whatever the chunk; the chunk is the pulse group that
- * shares one float-float reference (mid-chunk pulse).  staged=2 runs the staged kernel on a persistent grid
+ * or 2 with chunk 32, 64 or 128 and (tile, window, stage) 16x16/160/32,
+ * 16x16/160/16, 16x16/128/32, 16x8/128/32, 16x8/128/16, 32x8/128/32,
+ * 64x4/128/32.  The staged kernels copy raw data in 16- or 32-pulse stages
+ * through a ring of 64 pulses; the chunk is the pulse group that shares one
+ * float-float reference (mid-chunk pulse).  staged=2 runs the staged kernel on a persistent grid
  * that drains a queue of the scene's tiles in decreasing estimated cost; the
  * queue (built by sarbp_mixed_prepare) adds a few bytes per tile to the
  * workspace.  Images are bit-identical across staged=1 and staged=2.
@@ -89,8 +90,9 @@ typedef struct sarbp_tuning {
     int32_t staged;       /* 0: L1/L2 gathers; 1: TMA-staged raw window, one CTA per
                              tile; 2: staged, persistent grid over a cost-ordered
                              tile queue */
-    int32_t window;       /* staged: range bins staged per pulse chunk (0: default) */
-    int32_t reserved[3];
+    int32_t window;       /* staged: range bins staged per pulse stage (0: default) */
+    int32_t stage;        /* staged: pulses per TMA stage, 16 or 32 (0: default)   */
+    int32_t reserved[2];
 } sarbp_tuning;
 
 /* Device counters written by the mixed kernel when `counters` is non-NULL. */

@@ -52,12 +52,13 @@ class Tuning(C.Structure):
 
     _fields_ = [
         ("chunk", C.c_int32), ("tile0", C.c_int32), ("tile1", C.c_int32),
-        ("staged", C.c_int32), ("window", C.c_int32), ("reserved", C.c_int32 * 3),
+        ("staged", C.c_int32), ("window", C.c_int32), ("stage", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
     def as_dict(self) -> dict:
         return {"chunk": self.chunk, "tile0": self.tile0, "tile1": self.tile1,
-                "staged": self.staged, "window": self.window}
+                "staged": self.staged, "window": self.window, "stage": self.stage}
 
 
 _P = C.c_void_p

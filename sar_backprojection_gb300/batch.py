@@ -30,9 +30,10 @@ from .scene import DeviceScene
 STAGED_TILINGS = ((16, 16, 128), (16, 16, 160), (16, 8, 128), (32, 8, 128), (64, 4, 128))
 
 
-def staged_tuning(tile0: int = 16, tile1: int = 16, window: int = 160) -> _lib.Tuning:
-    return resolve_tuning({"chunk": 32, "tile0": tile0, "tile1": tile1, "staged": 1,
-                           "window": window})
+def staged_tuning(tile0: int = 16, tile1: int = 16, window: int = 160, chunk: int = 32,
+                  stage: int = 32) -> _lib.Tuning:
+    return resolve_tuning({"chunk": chunk, "tile0": tile0, "tile1": tile1, "staged": 1,
+                           "window": window, "stage": stage})
 
 
 def _stream_ptr(device) -> int:
@@ -66,8 +67,8 @@ class BatchFocuser:
         self.lib = _lib.load()
         self.device = scenes[0].device
         self.tuning = staged_tuning() if tuning is None else resolve_tuning(tuning)
-        if not self.tuning.staged or self.tuning.chunk != 32:
-            raise ValueError("the batch path runs the staged kernel (staged=1, chunk=32)")
+        if not self.tuning.staged or self.tuning.chunk not in (32, 64, 128):
+            raise ValueError("the batch path runs the staged kernel (staged=1, chunk 32/64/128)")
         # the batch has its own (scene, tile) queue: no per-scene tile queue
         self.tuning.staged = 1
         self.diagnostics = diagnostics

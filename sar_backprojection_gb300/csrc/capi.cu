@@ -116,6 +116,11 @@ bool valid_tuning(sarbp_tuning *t)
         t->tile1 = 16;
     }
     if (t->staged && t->window == 0) t->window = (t->tile0 * t->tile1 >= 256) ? 160 : 128;
+    if (t->stage == 0) t->stage = 32;
+    if (t->stage != 16 && t->stage != 32) {
+        set_error("tuning.stage must be 16 or 32 (got %d)", t->stage);
+        return false;
+    }
     if (t->staged < 0 || t->staged > 2) {
         set_error("tuning.staged must be 0, 1 or 2 (got %d)", t->staged);
         return false;

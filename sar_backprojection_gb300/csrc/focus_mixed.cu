@@ -30,7 +30,7 @@ MixedLayout mixed_layout(const SceneParams &P, const sarbp_tuning &T)
     L.ctab = off;
     off = align256(off + sizeof(ChunkRef) * (size_t)nchunks);
     L.sdev = off;
-    off = align256(off + sizeof(float) * (size_t)(nchunks * chunk / 32));
+    off = align256(off + sizeof(float) * (size_t)(nchunks * chunk / (T.stage > 0 ? T.stage : 32)));
     L.base = off;
     if (T.staged == 2 && T.tile0 > 0 && T.tile1 > 0) {
         const int64_t nt = ((P.dim0 + T.tile0 - 1) / T.tile0) * ((P.dim1 + T.tile1 - 1) / T.tile1);
@@ -77,7 +77,7 @@ __device__ __forceinline__ void store_e(float4 *ptab, int64_t k, float4 e, bool 
 }
 
 // Per-pulse tables and per-chunk references; one warp per chunk.
-__global__ void chunk_table_kernel(const SceneParams P, int chunk, int paired,
+__global__ void chunk_table_kernel(const SceneParams P, int chunk, int stage, int paired,
                                    float4 *__restrict__ ptab, PulseFF *__restrict__ pff,
                                    ChunkRef *__restrict__ ctab, float *__restrict__ sdev,
                                    int64_t nchunks)
@@ -126,13 +126,13 @@ __global__ void chunk_table_kernel(const SceneParams P, int chunk, int paired,
         const double rx = qx - u * sx, ry = qy - u * sy, rz = qz - u * sz;
         dev = fmax(dev, sqrt(rx * rx + ry * ry + rz * rz));
     }
-    // The same per 32-pulse stage (the staged kernel's TMA unit): one pulse
-    // per lane.
-    for (int s = 0; s < chunk / 32; ++s) {
-        const int64_t sa = c * chunk + s * 32;
+    // The same per stage of `stage` pulses (the staged kernels' TMA unit):
+    // one pulse per lane.
+    for (int s = 0; s < chunk / stage; ++s) {
+        const int64_t sa = c * chunk + s * stage;
         double sd = 0.0;
         if (sa < P.naz) {
-            const int64_t sb = min(sa + 31, P.naz - 1);
+            const int64_t sb = min(sa + stage - 1, P.naz - 1);
             const double bx = P.tx[sa], by = P.ty[sa], bz = P.tz[sa];
             const double vx = P.tx[sb] - bx, vy = P.ty[sb] - by, vz = P.tz[sb] - bz;
             const double vv = vx * vx + vy * vy + vz * vz;
@@ -145,7 +145,7 @@ __global__ void chunk_table_kernel(const SceneParams P, int chunk, int paired,
             }
         }
         for (int o = 16; o > 0; o >>= 1) sd = fmax(sd, __shfl_xor_sync(0xffffffffu, sd, o));
-        if (lane == 0) sdev[c * (chunk / 32) + s] = (float)sd + 1.0e-3f;   // + margin (m)
+        if (lane == 0) sdev[c * (chunk / stage) + s] = (float)sd + 1.0e-3f;   // + margin (m)
     }
     for (int o = 16; o > 0; o >>= 1) {
         mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -337,15 +337,16 @@ int launch_staged(const SceneParams &P, const sarbp_tuning &T, const MixedLayout
                   bool queued, double *out, int32_t *nvalid, uint64_t *checksum,
                   uint64_t *counters, cudaStream_t stream);
 
-int launch_chunk_table(const SceneParams &P, int chunk, bool paired, char *ws,
+int launch_chunk_table(const SceneParams &P, int chunk, int stage, bool paired, char *ws,
                        const MixedLayout &L, cudaStream_t stream)
 {
     const int64_t nchunks = (P.naz + chunk - 1) / chunk;
     const int warps = 8;
     const int64_t blocks = (nchunks + warps - 1) / warps;
     chunk_table_kernel<<<(unsigned)blocks, warps * 32, 0, stream>>>(
-        P, chunk, paired ? 1 : 0, reinterpret_cast<float4 *>(ws + L.ptab), reinterpret_cast<PulseFF *>(ws + L.pff),
-        reinterpret_cast<ChunkRef *>(ws + L.ctab), reinterpret_cast<float *>(ws + L.sdev), nchunks);
+        P, chunk, stage, paired ? 1 : 0, reinterpret_cast<float4 *>(ws + L.ptab),
+        reinterpret_cast<PulseFF *>(ws + L.pff), reinterpret_cast<ChunkRef *>(ws + L.ctab),
+        reinterpret_cast<float *>(ws + L.sdev), nchunks);
     return cuda_status(cudaGetLastError(), "chunk_table launch");
 }
 
@@ -367,7 +368,7 @@ int launch_mixed_prepare(const SceneParams &P, const sarbp_tuning &T, void *work
     if (rc) return rc;
     char *ws = static_cast<char *>(workspace);
     // the staged kernels read the pair-interleaved table (f32x2 operands)
-    rc = launch_chunk_table(P, T.chunk, T.staged != 0, ws, L, stream);
+    rc = launch_chunk_table(P, T.chunk, T.stage > 0 ? T.stage : 32, T.staged != 0, ws, L, stream);
     if (rc) return rc;
     // persistent staged path: tiles in decreasing estimated cost
     if (T.staged == 2) return tile_order(P, T, L, ws, stream);

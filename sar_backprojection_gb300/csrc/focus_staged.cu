@@ -120,7 +120,7 @@ int batch_set_scene(void *bws, size_t bytes, int slot, int nscenes, const SceneP
     }
     BatchScene B;
     memset(&B, 0, sizeof(B));
-    int rc = make_raw_map(P, T.window, kStage, &B.map);
+    int rc = make_raw_map(P, T.window, T.stage, &B.map);
     if (rc) return rc;
     B.P = P;
     B.tables = tables_of(static_cast<char *>(scene_ws), L);

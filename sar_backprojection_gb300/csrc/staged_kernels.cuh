@@ -4,19 +4,22 @@
 // staged_c32.cu, staged_c64.cu, staged_c128.cu).
 //
 // Same decomposition and precision plan as the gather kernel
-// (focus_mixed.cu, mixed_common.cuh), but each CTA stages, per 32-pulse
-// stage, the range window its pixel tile can touch into shared memory with
-// one 2-D tiled TMA load (box = W range bins x 32 pulses of the pulse-major
-// raw data) plus a 1-D bulk copy of the stage's per-pulse table, double
-// buffered: while the CTA focuses stage c from buffer c&1, the copies of
-// stage c+1 land in the other buffer.  The per-pulse gathers then hit shared
-// memory instead of L1/L2.
+// (focus_mixed.cu, mixed_common.cuh), but each CTA stages, per STAGE-pulse
+// stage (16 or 32 pulses), the range window its pixel tile can touch into
+// shared memory with one 2-D tiled TMA load (box = W range bins x STAGE
+// pulses of the pulse-major raw data) plus a 1-D bulk copy of the stage's
+// per-pulse table.  NBUF = 64 / STAGE buffers form a ring: a warp that has
+// finished a stage releases its buffer (a shared counter), and the last warp
+// to release it issues the copies of the stage NBUF ahead into it.  Warps are
+// never held in lock step by a CTA barrier inside a pass; a warp runs at most
+// NBUF - 1 stages ahead of the slowest.
 //
 // The float-float reference (chunk_setup) is computed once per chunk of
 // CHUNK = 32, 64 or 128 pulses (reference pulse mid-chunk), before the wait
-// for the chunk's first stage; a chunk's stages sum
-// into one FP32 partial that is rotated by the reference phasor and added to
-// the Kahan accumulator once per chunk.
+// for the chunk's first stage; a chunk's stages sum into one FP32 partial
+// that is rotated by the reference phasor and added to the Kahan accumulator
+// once per chunk.  The fast path evaluates two pulses per packed f32x2
+// instruction.
 //
 // The window of stage c is the range-bin interval every pixel of the tile can
 // reach from the stage's pulses: per pixel, the distances to the stage's
@@ -26,9 +29,10 @@
 // window (a window wider than W) is read from global memory instead and
 // counted as a window miss, so correctness never depends on the window.
 //
-// All mbarrier waits are bounded; a wait that gives up marks the workspace
-// status block and the CTA leaves after its last copy lands (or after a
-// second bounded wait).
+// All mbarrier waits are bounded; a wait that gives up sets the CTA's stop
+// flag, every warp leaves the pass, and the CTA marks the workspace status
+// block and exits after the copies it issued have landed (or after a second
+// bounded wait).
 #include <algorithm>
 #include <climits>
 #include <cstdio>
@@ -43,17 +47,25 @@
 
 namespace sarbp {
 
-constexpr int kStage = 32;                 // pulses per TMA stage
-constexpr int kMaxPassChunks = 128;        // stages whose windows are kept at once
+constexpr int kMaxPassStages = 128;        // stages whose windows are kept at once
+constexpr int kMaxBuf = 4;                 // ring buffers (64 pulses / 16-pulse stages)
 constexpr uint32_t kWaitLimit = 1u << 22;  // mbarrier polls before giving up
 
-template <int CHUNK, int W>
-struct StagedSmem {
-    static_assert(CHUNK % kStage == 0 && kMaxPassChunks % (CHUNK / kStage) == 0, "chunk");
-    static constexpr size_t raw_bytes = (size_t)kStage * W * sizeof(float2);
-    static constexpr size_t tab_bytes = (size_t)kStage * sizeof(float4);
-    static constexpr size_t stage_bytes = raw_bytes + tab_bytes;
-    static constexpr size_t bytes = 2 * stage_bytes + 128;    // + alignment slack
+// Compile-time shape of a staged variant.
+template <int CHUNK_, int T0_, int T1_, int W_, int STAGE_>
+struct StagedCfg {
+    static constexpr int CHUNK = CHUNK_, T0 = T0_, T1 = T1_, W = W_, STAGE = STAGE_;
+    static constexpr int NBUF = 64 / STAGE;        // 64 pulses of raw windows in flight
+    static constexpr int R = CHUNK / STAGE;        // stages per chunk
+    static constexpr int THREADS = T0 * T1, WARPS = THREADS / 32;
+    static constexpr size_t raw_bytes = (size_t)STAGE * W * sizeof(float2);
+    static constexpr size_t tab_bytes = (size_t)STAGE * sizeof(float4);
+    static constexpr size_t buf_bytes = raw_bytes + tab_bytes;
+    static constexpr size_t smem_bytes = NBUF * buf_bytes + 128;   // + alignment slack
+    static_assert(STAGE == 16 || STAGE == 32, "stage");
+    static_assert(NBUF <= kMaxBuf && (NBUF & (NBUF - 1)) == 0, "ring");
+    static_assert(CHUNK % STAGE == 0 && kMaxPassStages % R == 0, "chunk");
+    static_assert(buf_bytes % 128 == 0, "TMA destinations stay 128-byte aligned");
 };
 
 template <int T0, int T1>
@@ -114,17 +126,24 @@ __device__ __forceinline__ void safe_setup(ChunkSetup &S, int b0)
     S.exact = false;
 }
 
-// Shared-memory state of one CTA of a staged kernel.  It persists across the
-// tiles a persistent CTA processes: the stage counter keeps the mbarrier
-// phases in step.
+// Static shared memory of a staged CTA.  It persists across the tiles a
+// persistent CTA processes: the stage counter keeps the ring's mbarrier
+// phases and release counts in step.
+struct StagedShared {
+    uint64_t full_bar[kMaxBuf];       // copy completion per buffer
+    unsigned rel[kMaxBuf];            // warps done with a buffer (cumulative)
+    unsigned last_parity[kMaxBuf];    // phase parity of the last copy into a buffer
+    int issued[kMaxBuf];              // a copy was ever issued into the buffer
+    int stop;                         // a bounded wait gave up
+    int wlo[kMaxPassStages], whi[kMaxPassStages];   // range windows of a pass
+    long long lo, hi;                 // tile-wide pulse range
+    long long item[2];                // persistent kernels: current work item
+};
+
 struct StagedCta {
-    unsigned char *smem;       // 2 stages, 1024-byte aligned
-    uint64_t *full_bar;        // [2] copy-completion barriers
-    int *s_wlo, *s_whi;        // [kMaxPassChunks] range windows of a pass
-    long long *s_lo, *s_hi;    // tile-wide pulse range
-    uint32_t it;               // chunk iteration counter (stage = it & 1)
-    bool pending[2];           // thread 0: copies in flight per stage
-    uint32_t pending_parity[2];
+    unsigned char *smem;       // NBUF buffers, 128-byte aligned
+    StagedShared *sh;
+    uint32_t it;               // stage counter (buffer = it % NBUF)
 };
 
 struct TileTables {
@@ -155,24 +174,24 @@ struct BatchScene {
 
 // Focus one pixel tile; false if a bounded wait gave up (the CTA must stop).
 // Every thread of the CTA calls it with the same tile.
-template <int CHUNK, int T0, int T1, int W, bool kChecksum>
+template <class Cfg, bool kChecksum>
 __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P,
                                             const CUtensorMap *raw_map, const TileTables &tb,
                                             int64_t tile0, int64_t tile1, const TileOutputs &o,
                                             TileStats &st)
 {
-    using SM = StagedSmem<CHUNK, W>;
+    constexpr int W = Cfg::W, STAGE = Cfg::STAGE, NBUF = Cfg::NBUF, R = Cfg::R;
+    constexpr int CHUNK = Cfg::CHUNK;
     unsigned char *smem = cta.smem;
-    uint64_t *full_bar = cta.full_bar;
-    int *s_wlo = cta.s_wlo, *s_whi = cta.s_whi;
+    StagedShared &sh = *cta.sh;
     const float4 *ptab = tb.ptab;
     const PulseFF *pff = tb.pff;
     const ChunkRef *ctab = tb.ctab;
     const float *sdev = tb.sdev;
 
-    const int t = threadIdx.x;
+    const int t = threadIdx.x, lane = t & 31;
     int64_t i0, i1;
-    staged_tile_pixel<T0, T1>(t, tile0, tile1, i0, i1);
+    staged_tile_pixel<Cfg::T0, Cfg::T1>(t, tile0, tile1, i0, i1);
     const bool inside = i0 < P.dim0 && i1 < P.dim1;
     const int64_t ii = inside ? i0 + P.dim0 * i1 : 0;
     int64_t lo = 0, hi = -1;
@@ -180,16 +199,16 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
         inside && pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi);
 
     if (t == 0) {
-        *cta.s_lo = LLONG_MAX;
-        *cta.s_hi = -1;
+        sh.lo = LLONG_MAX;
+        sh.hi = -1;
     }
     __syncthreads();
     if (active) {
-        atomicMin(cta.s_lo, (long long)lo);
-        atomicMax(cta.s_hi, (long long)hi);
+        atomicMin(&sh.lo, (long long)lo);
+        atomicMax(&sh.hi, (long long)hi);
     }
     __syncthreads();
-    const int64_t tlo = *cta.s_lo, thi = *cta.s_hi;
+    const int64_t tlo = sh.lo, thi = sh.hi;
 
     PixelFF pf{};
     if (active) pf = pixel_ff(P.x[ii], P.y[ii], P.z[ii]);
@@ -199,31 +218,27 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
     unsigned ambiguous = 0, chunks = 0, misses = 0;
     const unsigned nra_m1 = (unsigned)(P.nra - 1);
     const int pitch = (int)P.pitch;
-    uint32_t &it = cta.it;
-    bool *pending = cta.pending;
-    uint32_t *pending_parity = cta.pending_parity;
-    bool aborted = false;
-    constexpr int R = CHUNK / kStage;     // stages per chunk (setup group)
+    bool stopped = false;
     ChunkSetup S;
     safe_setup(S, 0);
     bool gwork = false;                   // pixel has pulses in the current chunk
     int64_t cur_chunk = -1;
     float gre = 0.f, gim = 0.f;           // FP32 partial sum of the current chunk
     if (thi >= 0) {
-        const int64_t c_first = tlo / kStage, c_last = thi / kStage;
-        for (int64_t cb = c_first; cb <= c_last && !aborted; cb += kMaxPassChunks) {
-            const int npass = (int)min((int64_t)kMaxPassChunks, c_last - cb + 1);
+        const int64_t c_first = tlo / STAGE, c_last = thi / STAGE;
+        for (int64_t cb = c_first; cb <= c_last && !stopped; cb += kMaxPassStages) {
+            const int npass = (int)min((int64_t)kMaxPassStages, c_last - cb + 1);
             // ---- window prologue: bins every pixel can reach per stage ----
             for (int q = t; q < npass; q += blockDim.x) {
-                s_wlo[q] = INT_MAX;
-                s_whi[q] = INT_MIN;
+                sh.wlo[q] = INT_MAX;
+                sh.whi[q] = INT_MIN;
             }
             __syncthreads();
             for (int q = 0; q < npass; ++q) {
-                const int64_t K = (cb + q) * kStage;
+                const int64_t K = (cb + q) * STAGE;
                 int blo = INT_MAX, bhi = INT_MIN;
-                if (active && lo <= K + kStage - 1 && hi >= K) {
-                    const int64_t ka = K, kb = min(K + kStage - 1, P.naz - 1);
+                if (active && lo <= K + STAGE - 1 && hi >= K) {
+                    const int64_t ka = K, kb = min(K + STAGE - 1, P.naz - 1);
                     const float4 ta = __ldg(&pff[ka].hi), tb = __ldg(&pff[kb].hi);
                     const float dev = __ldg(&sdev[cb + q]);
                     const float ax = pf.xh - ta.x, ay = pf.yh - ta.y, az = pf.zh - ta.z;
@@ -250,37 +265,43 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                     blo = min(blo, __shfl_xor_sync(0xffffffffu, blo, o));
                     bhi = max(bhi, __shfl_xor_sync(0xffffffffu, bhi, o));
                 }
-                if ((t & 31) == 0 && blo <= bhi) {
-                    atomicMin(&s_wlo[q], blo);
-                    atomicMax(&s_whi[q], bhi);
+                if (lane == 0 && blo <= bhi) {
+                    atomicMin(&sh.wlo[q], blo);
+                    atomicMax(&sh.whi[q], bhi);
                 }
             }
             __syncthreads();
 
-            // ---- producer: stage q of this pass into buffer s ----
             // window start of stage q: even (16-byte aligned TMA x coordinate),
             // inside [0, nra]; 0 for a stage no pixel of the tile reaches
             auto window_start = [&](int q) {
-                const int wl = s_wlo[q], wh = s_whi[q];
+                const int wl = sh.wlo[q], wh = sh.whi[q];
                 if (wl > wh) return 0;
                 return (int)min((int64_t)max(wl, 0), P.nra) & ~1;
             };
-            auto issue = [&](int q, int s, uint32_t use) {
-                unsigned char *base = smem + (size_t)s * SM::stage_bytes;
-                const int64_t K = (cb + q) * kStage;
-                mbar_arrive_expect_tx(&full_bar[s], (uint32_t)SM::stage_bytes);
-                tma_load_2d(base, raw_map, &full_bar[s], window_start(q), (int)K);
-                bulk_load(base + SM::raw_bytes, ptab + K, (uint32_t)SM::tab_bytes, &full_bar[s]);
-                pending[s] = true;
-                pending_parity[s] = use & 1;
+            // copies of stage q of this pass into buffer b (any single thread)
+            auto issue = [&](int q, int b, uint32_t use) {
+                unsigned char *base = smem + (size_t)b * Cfg::buf_bytes;
+                const int64_t K = (cb + q) * STAGE;
+                mbar_arrive_expect_tx(&sh.full_bar[b], (uint32_t)Cfg::buf_bytes);
+                tma_load_2d(base, raw_map, &sh.full_bar[b], window_start(q), (int)K);
+                bulk_load(base + Cfg::raw_bytes, ptab + K, (uint32_t)Cfg::tab_bytes,
+                          &sh.full_bar[b]);
+                sh.last_parity[b] = use & 1;
+                sh.issued[b] = 1;
             };
-            if (t == 0) issue(0, it & 1, it >> 1);
+            const uint32_t it0 = cta.it;
+            // every buffer is free at a pass start: prime the ring
+            if (t == 0)
+                for (int q = 0; q < NBUF && q < npass; ++q)
+                    issue(q, (int)((it0 + q) % NBUF), (it0 + q) / NBUF);
 
-            for (int q = 0; q < npass; ++q, ++it) {
-                const int s = it & 1;
-                if (t == 0 && q + 1 < npass) issue(q + 1, s ^ 1, (it + 1) >> 1);
+            for (int q = 0; q < npass; ++q) {
+                const uint32_t itq = it0 + (uint32_t)q;
+                const int b = (int)(itq % NBUF);
+                const uint32_t use = itq / NBUF;
                 const int64_t c = cb + q;
-                const int64_t K = c * kStage;
+                const int64_t K = c * STAGE;
                 // ---- chunk reference: once per CHUNK pulses, before the wait ----
                 const int64_t chunk = c / R;
                 if (chunk != cur_chunk) {
@@ -299,23 +320,27 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                         safe_setup(S, 0);
                     }
                 }
-                const bool ready = mbar_wait(&full_bar[s], (it >> 1) & 1, kWaitLimit);
-                if (t == 0 && ready) pending[s] = false;
+                const bool ready = mbar_wait(&sh.full_bar[b], use & 1, kWaitLimit);
+                if (!ready) *(volatile int *)&sh.stop = 1;
+                if (__any_sync(0xffffffffu, !ready) || *(volatile int *)&sh.stop) {
+                    stopped = true;
+                    break;
+                }
                 const int jmin = (int)(lo > K ? lo - K : 0);
-                const int jmax = (int)(hi < K + kStage - 1 ? hi - K : kStage - 1);
-                const bool work = ready && gwork && jmin <= jmax;
+                const int jmax = (int)(hi < K + STAGE - 1 ? hi - K : STAGE - 1);
+                const bool work = gwork && jmin <= jmax;
                 const float2 *sraw =
-                    reinterpret_cast<const float2 *>(smem + (size_t)s * SM::stage_bytes);
+                    reinterpret_cast<const float2 *>(smem + (size_t)b * Cfg::buf_bytes);
                 const float4 *stab = reinterpret_cast<const float4 *>(
-                    smem + (size_t)s * SM::stage_bytes + SM::raw_bytes);
+                    smem + (size_t)b * Cfg::buf_bytes + Cfg::raw_bytes);
                 const int b0 = window_start(q);
                 // window covers every bin the tile can reach and lies inside
                 // the kept bins 0..nra-2: no per-pulse validity/window tests
-                const bool win_ok = s_wlo[q] >= 0 && (int64_t)s_whi[q] <= P.nra - 2 &&
-                                    s_whi[q] - b0 < W;
+                const bool win_ok = sh.wlo[q] >= 0 && (int64_t)sh.whi[q] <= P.nra - 2 &&
+                                    sh.whi[q] - b0 < W;
                 const bool exact = work && S.exact;
                 const bool fast = __all_sync(0xffffffffu, !work || (jmin == 0 &&
-                                                                    jmax == kStage - 1 &&
+                                                                    jmax == STAGE - 1 &&
                                                                     win_ok && !exact));
                 if (!__any_sync(0xffffffffu, work)) {
                     // no pixel of this warp has pulses in the stage
@@ -353,7 +378,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                         const ulonglong2 *sp = reinterpret_cast<const ulonglong2 *>(stab);
                         float rmax = 0.f;     // largest |g - rint(g)|: a tie test per stage
 #pragma unroll
-                        for (int p = 0; p < kStage / 2; ++p) {
+                        for (int p = 0; p < STAGE / 2; ++p) {
                             const ulonglong2 exy = sp[2 * p], ezw = sp[2 * p + 1];
                             f2_t D2 = f2_fma(mz2, ezw.x, ezw.y);
                             D2 = f2_fma(my2, exy.y, D2);
@@ -394,7 +419,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                         }
                         if (work && rmax > tie) {
                             // a pulse near a .5 tie (rare): find which
-                            for (int j = 0; j < kStage; ++j) {
+                            for (int j = 0; j < STAGE; ++j) {
                                 float D, dR;
                                 int col;
                                 bool amb;
@@ -410,7 +435,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                                     ~((1u << jmin) - 1u))
                                  : 0u;
 #pragma unroll
-                        for (int j = 0; j < kStage; ++j) {
+                        for (int j = 0; j < STAGE; ++j) {
                             float D, dR;
                             int col;
                             bool amb;
@@ -494,19 +519,28 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                     kahan_add(acc_im, cmp_im, rim);
                     gre = gim = 0.f;
                 }
-                // every thread is done with buffer s before it is refilled
-                if (__syncthreads_or(!ready)) {
-                    aborted = true;
-                    break;
+                // release buffer b; the last warp to release it refills it
+                __syncwarp();
+                if (lane == 0) {
+                    __threadfence_block();
+                    const unsigned old = atomicAdd(&sh.rel[b], 1u);
+                    if (old % Cfg::WARPS == Cfg::WARPS - 1 && q + NBUF < npass) {
+                        __threadfence_block();
+                        fence_proxy_async_smem();
+                        issue(q + NBUF, b, use + 1);
+                    }
                 }
             }
+            __syncthreads();                  // end of pass: every warp left the ring
+            if (*(volatile int *)&sh.stop) stopped = true;
+            cta.it = it0 + (uint32_t)npass;
         }
     }
 
     st.ambiguous += ambiguous;
     st.chunks += chunks;
     st.misses += misses;
-    if (aborted) return false;
+    if (stopped) return false;
     if (inside) {
         double2 res = make_double2(0.0, 0.0);
         if (n > 0) {
@@ -521,42 +555,44 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
     return true;
 }
 
-template <int CHUNK, int W>
-__device__ __forceinline__ StagedCta staged_cta_init(unsigned char *smem_dyn, uint64_t *full_bar,
-                                                     int *s_wlo, int *s_whi, long long *s_lo,
-                                                     long long *s_hi)
+template <class Cfg>
+__device__ __forceinline__ StagedCta staged_cta_init(unsigned char *smem_dyn, StagedShared &sh)
 {
     StagedCta cta;
     // TMA tile loads without swizzle need 128-byte aligned destinations
     cta.smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_dyn) + 127) & ~(uintptr_t)127);
-    cta.full_bar = full_bar;
-    cta.s_wlo = s_wlo;
-    cta.s_whi = s_whi;
-    cta.s_lo = s_lo;
-    cta.s_hi = s_hi;
+    cta.sh = &sh;
     cta.it = 0;
-    cta.pending[0] = cta.pending[1] = false;
-    cta.pending_parity[0] = cta.pending_parity[1] = 0;
     if (threadIdx.x == 0) {
-        mbar_init(&full_bar[0], 1);
-        mbar_init(&full_bar[1], 1);
+        for (int b = 0; b < Cfg::NBUF; ++b) {
+            mbar_init(&sh.full_bar[b], 1);
+            sh.rel[b] = 0;
+            sh.last_parity[b] = 0;
+            sh.issued[b] = 0;
+        }
+        sh.stop = 0;
         mbar_fence_init();
     }
     __syncthreads();
     return cta;
 }
 
-// A bounded wait gave up: mark the status block and let copies still in
-// flight land before the CTA's shared memory goes away.
+// A bounded wait gave up: mark the status block and let the last copy issued
+// into each buffer land before the CTA's shared memory goes away (at most one
+// copy per buffer is ever in flight).  Called by every thread after the
+// tile returned false.
+template <class Cfg>
 __device__ __forceinline__ void staged_abort(StagedCta &cta, StatusBlock *status,
                                              unsigned long long *counters)
 {
+    __syncthreads();
     if (threadIdx.x == 0) {
+        StagedShared &sh = *cta.sh;
         atomicOr(&status->error, 1u);
         atomicExch(&status->where, 1u);
-        for (int s = 0; s < 2; ++s)
-            if (cta.pending[s]) mbar_wait(&cta.full_bar[s], cta.pending_parity[s], kWaitLimit);
+        for (int b = 0; b < Cfg::NBUF; ++b)
+            if (sh.issued[b]) mbar_wait(&sh.full_bar[b], sh.last_parity[b], kWaitLimit);
         if (counters) atomicAdd(counters + SARBP_CTR_TIMEOUTS, 1ull);
     }
 }
@@ -577,23 +613,29 @@ __device__ __forceinline__ void flush_stats(TileStats &st, unsigned long long *c
     }
 }
 
+// At least 512 threads' worth of CTAs per SM (at most 128 registers per
+// thread): two 256-thread CTAs fit the shared memory of every variant.
+template <class Cfg>
+constexpr int staged_min_blocks_single()
+{
+    return 512 / Cfg::THREADS > 2 ? 512 / Cfg::THREADS : 2;
+}
+
 // One scene: one CTA per pixel tile.
-template <int CHUNK, int T0, int T1, int W, bool kChecksum>
-__global__ void __launch_bounds__(T0 *T1)
+template <class Cfg, bool kChecksum>
+__global__ void __launch_bounds__(Cfg::THREADS, (staged_min_blocks_single<Cfg>()))
 focus_mixed_staged_kernel(const SceneParams P, const __grid_constant__ CUtensorMap raw_map,
                           const TileTables tb, int64_t ntile0, const TileOutputs o,
                           unsigned long long *__restrict__ counters, StatusBlock *status)
 {
     extern __shared__ unsigned char smem_dyn[];
-    __shared__ __align__(8) uint64_t full_bar[2];
-    __shared__ int s_wlo[kMaxPassChunks], s_whi[kMaxPassChunks];
-    __shared__ long long s_lo, s_hi;
-    StagedCta cta = staged_cta_init<CHUNK, W>(smem_dyn, full_bar, s_wlo, s_whi, &s_lo, &s_hi);
+    __shared__ StagedShared sh;
+    StagedCta cta = staged_cta_init<Cfg>(smem_dyn, sh);
     TileStats st{0, 0, 0};
-    const bool ok = staged_tile<CHUNK, T0, T1, W, kChecksum>(
-        cta, P, &raw_map, tb, blockIdx.x % ntile0, blockIdx.x / ntile0, o, st);
+    const bool ok = staged_tile<Cfg, kChecksum>(cta, P, &raw_map, tb, blockIdx.x % ntile0,
+                                                blockIdx.x / ntile0, o, st);
     if (!ok) {
-        staged_abort(cta, status, counters);
+        staged_abort<Cfg>(cta, status, counters);
         return;
     }
     flush_stats(st, counters);
@@ -602,8 +644,8 @@ focus_mixed_staged_kernel(const SceneParams P, const __grid_constant__ CUtensorM
 // One scene, persistent grid: CTAs pull tiles in decreasing estimated cost
 // (the order prepared in the workspace) until the queue is empty, so the
 // longest tiles start first and no wave of CTAs ends half empty.
-template <int CHUNK, int T0, int T1, int W, bool kChecksum>
-__global__ void __launch_bounds__(T0 *T1)
+template <class Cfg, bool kChecksum>
+__global__ void __launch_bounds__(Cfg::THREADS, (staged_min_blocks_single<Cfg>()))
 focus_mixed_staged_queue_kernel(const SceneParams P, const __grid_constant__ CUtensorMap raw_map,
                                 const TileTables tb, int64_t ntile0,
                                 const int32_t *__restrict__ order, int64_t ntiles,
@@ -611,65 +653,60 @@ focus_mixed_staged_queue_kernel(const SceneParams P, const __grid_constant__ CUt
                                 unsigned long long *__restrict__ counters, StatusBlock *status)
 {
     extern __shared__ unsigned char smem_dyn[];
-    __shared__ __align__(8) uint64_t full_bar[2];
-    __shared__ int s_wlo[kMaxPassChunks], s_whi[kMaxPassChunks];
-    __shared__ long long s_lo, s_hi;
-    __shared__ long long s_item[2];
-    StagedCta cta = staged_cta_init<CHUNK, W>(smem_dyn, full_bar, s_wlo, s_whi, &s_lo, &s_hi);
+    __shared__ StagedShared sh;
+    StagedCta cta = staged_cta_init<Cfg>(smem_dyn, sh);
     TileStats st{0, 0, 0};
     for (int round = 0;; ++round) {
-        if (threadIdx.x == 0) s_item[round & 1] = (long long)atomicAdd(cursor, 1ull);
+        if (threadIdx.x == 0) sh.item[round & 1] = (long long)atomicAdd(cursor, 1ull);
         __syncthreads();
-        const long long item = s_item[round & 1];
+        const long long item = sh.item[round & 1];
         if (item >= ntiles) break;
         const int64_t tile = order[item];
         if (tile < 0 || tile >= ntiles) continue;   // a queue prepared for other pixels
-        const bool ok = staged_tile<CHUNK, T0, T1, W, kChecksum>(
-            cta, P, &raw_map, tb, tile % ntile0, tile / ntile0, o, st);
+        const bool ok = staged_tile<Cfg, kChecksum>(cta, P, &raw_map, tb, tile % ntile0,
+                                                    tile / ntile0, o, st);
         if (!ok) {
-            staged_abort(cta, status, counters);
+            staged_abort<Cfg>(cta, status, counters);
             return;
         }
     }
     flush_stats(st, counters);
 }
 
+// CTAs per SM the shared memory of a variant allows (2 or 3): the register
+// budget the batch kernel is compiled for.
+template <class Cfg>
+constexpr int staged_min_blocks()
+{
+    return Cfg::smem_bytes * 3 + 3 * 1024 <= 227 * 1024 ? 3 : 2;
+}
+
 // Many scenes in one persistent launch: CTAs pull (scene, tile) work items
 // from a device queue (a list ordered by decreasing estimated cost and an
 // atomic cursor) until it is empty.
-// CTAs per SM the shared memory of a (CHUNK, W) variant allows (2 or 3),
-// the register budget the batch kernel is compiled for.
-template <int CHUNK, int W>
-constexpr int staged_min_blocks()
-{
-    return StagedSmem<CHUNK, W>::bytes * 3 + 3 * 1024 <= 227 * 1024 ? 3 : 2;
-}
-
-template <int CHUNK, int T0, int T1, int W, bool kChecksum>
-__global__ void __launch_bounds__(T0 *T1, (staged_min_blocks<CHUNK, W>()))
+template <class Cfg, bool kChecksum>
+__global__ void __launch_bounds__(Cfg::THREADS, (staged_min_blocks<Cfg>()))
 focus_batch_staged_kernel(const BatchScene *__restrict__ scenes, const int2 *__restrict__ items,
                           int64_t n_items, unsigned long long *cursor,
                           unsigned long long *__restrict__ counters, StatusBlock *status)
 {
     extern __shared__ unsigned char smem_dyn[];
-    __shared__ __align__(8) uint64_t full_bar[2];
-    __shared__ int s_wlo[kMaxPassChunks], s_whi[kMaxPassChunks];
-    __shared__ long long s_lo, s_hi;
-    __shared__ long long s_item[2];
-    StagedCta cta = staged_cta_init<CHUNK, W>(smem_dyn, full_bar, s_wlo, s_whi, &s_lo, &s_hi);
+    __shared__ StagedShared sh;
+    StagedCta cta = staged_cta_init<Cfg>(smem_dyn, sh);
     TileStats st{0, 0, 0};
     for (int round = 0;; ++round) {
-        if (threadIdx.x == 0) s_item[round & 1] = (long long)atomicAdd(cursor, 1ull);
+        if (threadIdx.x == 0) sh.item[round & 1] = (long long)atomicAdd(cursor, 1ull);
         __syncthreads();
-        const long long item = s_item[round & 1];
+        const long long item = sh.item[round & 1];
         if (item >= n_items) break;
         const int2 w = items[item];
         const BatchScene &B = scenes[w.x];
         const int64_t tile = w.y;
-        const bool ok = staged_tile<CHUNK, T0, T1, W, kChecksum>(
-            cta, B.P, &B.map, B.tables, tile % B.ntile0, tile / B.ntile0, B.outputs, st);
+        const bool ok = staged_tile<Cfg, kChecksum>(cta, B.P, &B.map, B.tables,
+                                                    tile % B.ntile0, tile / B.ntile0,
+                                                    B.outputs, st);
         if (!ok) {
-            staged_abort(cta, status, counters);
+            staged_abort<Cfg>(cta, status, counters);
             return;
         }
     }
@@ -703,25 +740,24 @@ inline BatchLayout batch_layout(int nscenes, int64_t max_items)
 // 2-D tensor map over the pulse-major raw data (focus_staged.cu).
 int make_raw_map(const SceneParams &P, int W, int rows, CUtensorMap *map);
 
-template <int CHUNK, int T0, int T1, int W>
+template <class Cfg>
 static int ensure_smem_attr()
 {
-    using SM = StagedSmem<CHUNK, W>;
     // per device: the attribute belongs to the function in each context
     static bool done[64] = {};
     int dev = 0;
     int rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
     if (rc) return rc;
     if (dev < 0 || dev >= 64 || done[dev]) return SARBP_OK;
-    const void *ks[6] = {(const void *)focus_mixed_staged_kernel<CHUNK, T0, T1, W, false>,
-                         (const void *)focus_mixed_staged_kernel<CHUNK, T0, T1, W, true>,
-                         (const void *)focus_mixed_staged_queue_kernel<CHUNK, T0, T1, W, false>,
-                         (const void *)focus_mixed_staged_queue_kernel<CHUNK, T0, T1, W, true>,
-                         (const void *)focus_batch_staged_kernel<CHUNK, T0, T1, W, false>,
-                         (const void *)focus_batch_staged_kernel<CHUNK, T0, T1, W, true>};
+    const void *ks[6] = {(const void *)focus_mixed_staged_kernel<Cfg, false>,
+                         (const void *)focus_mixed_staged_kernel<Cfg, true>,
+                         (const void *)focus_mixed_staged_queue_kernel<Cfg, false>,
+                         (const void *)focus_mixed_staged_queue_kernel<Cfg, true>,
+                         (const void *)focus_batch_staged_kernel<Cfg, false>,
+                         (const void *)focus_batch_staged_kernel<Cfg, true>};
     for (const void *k : ks) {
         rc = cuda_status(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)SM::bytes),
+                                              (int)Cfg::smem_bytes),
                          "staged smem attribute");
         if (rc) return rc;
     }
@@ -739,12 +775,12 @@ inline TileTables tables_of(char *ws, const MixedLayout &L)
     return tb;
 }
 
-template <int CHUNK, int T0, int T1, int W>
+template <class Cfg>
 int launch_staged_t(const SceneParams &P, const MixedLayout &L, char *ws, bool queued,
                     double *out, int32_t *nvalid, uint64_t *checksum, uint64_t *counters,
                     cudaStream_t stream)
 {
-    using SM = StagedSmem<CHUNK, W>;
+    constexpr int T0 = Cfg::T0, T1 = Cfg::T1;
     const int64_t nt0 = (P.dim0 + T0 - 1) / T0, nt1 = (P.dim1 + T1 - 1) / T1;
     const int64_t tiles = nt0 * nt1;
     if (tiles > 0x7fffffffLL) {
@@ -752,51 +788,52 @@ int launch_staged_t(const SceneParams &P, const MixedLayout &L, char *ws, bool q
         return SARBP_ERANGE;
     }
     CUtensorMap map;
-    int rc = make_raw_map(P, W, kStage, &map);
+    int rc = make_raw_map(P, Cfg::W, Cfg::STAGE, &map);
     if (rc) return rc;
-    rc = ensure_smem_attr<CHUNK, T0, T1, W>();
+    rc = ensure_smem_attr<Cfg>();
     if (rc) return rc;
     const TileTables tb = tables_of(ws, L);
     const TileOutputs o{reinterpret_cast<double2 *>(out), nvalid, checksum};
     auto *status = reinterpret_cast<StatusBlock *>(ws + L.status);
     auto *ctr = reinterpret_cast<unsigned long long *>(counters);
     if (!queued) {
-        auto *k = checksum ? focus_mixed_staged_kernel<CHUNK, T0, T1, W, true>
-                           : focus_mixed_staged_kernel<CHUNK, T0, T1, W, false>;
-        k<<<(unsigned)tiles, T0 * T1, SM::bytes, stream>>>(P, map, tb, nt0, o, ctr, status);
+        auto *k = checksum ? focus_mixed_staged_kernel<Cfg, true>
+                           : focus_mixed_staged_kernel<Cfg, false>;
+        k<<<(unsigned)tiles, Cfg::THREADS, Cfg::smem_bytes, stream>>>(P, map, tb, nt0, o, ctr,
+                                                                       status);
         return cuda_status(cudaGetLastError(), "focus_mixed_staged launch");
     }
-    auto *k = checksum ? focus_mixed_staged_queue_kernel<CHUNK, T0, T1, W, true>
-                       : focus_mixed_staged_queue_kernel<CHUNK, T0, T1, W, false>;
+    auto *k = checksum ? focus_mixed_staged_queue_kernel<Cfg, true>
+                       : focus_mixed_staged_queue_kernel<Cfg, false>;
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, T0 * T1, SM::bytes),
+    rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, Cfg::THREADS,
+                                                                   Cfg::smem_bytes),
                      "queue occupancy");
     if (rc) return rc;
     const int64_t grid = std::min<int64_t>(tiles, (int64_t)std::max(1, per_sm) * sms);
     auto *cursor = reinterpret_cast<unsigned long long *>(ws + L.cursor);
     rc = cuda_status(cudaMemsetAsync(cursor, 0, sizeof(*cursor), stream), "queue cursor reset");
     if (rc) return rc;
-    k<<<(unsigned)grid, T0 * T1, SM::bytes, stream>>>(
+    k<<<(unsigned)grid, Cfg::THREADS, Cfg::smem_bytes, stream>>>(
         P, map, tb, nt0, reinterpret_cast<const int32_t *>(ws + L.vals_out), tiles, cursor, o,
         ctr, status);
     return cuda_status(cudaGetLastError(), "focus_mixed_staged_queue launch");
 }
 
-template <int C, int A, int B, int W>
+template <class Cfg>
 int launch_batch_t(char *bws, const BatchLayout &BL, int64_t n_items, bool diag,
-                          uint64_t *counters, cudaStream_t stream)
+                   uint64_t *counters, cudaStream_t stream)
 {
-    using SM = StagedSmem<C, W>;
-    int rc = ensure_smem_attr<C, A, B, W>();
+    int rc = ensure_smem_attr<Cfg>();
     if (rc) return rc;
-    auto *k = diag ? focus_batch_staged_kernel<C, A, B, W, true>
-                   : focus_batch_staged_kernel<C, A, B, W, false>;
+    auto *k = diag ? focus_batch_staged_kernel<Cfg, true> : focus_batch_staged_kernel<Cfg, false>;
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, A * B, SM::bytes),
+    rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, Cfg::THREADS,
+                                                                   Cfg::smem_bytes),
                      "batch occupancy");
     if (rc) return rc;
     const int64_t grid = std::min<int64_t>(n_items, (int64_t)std::max(1, per_sm) * sms);
@@ -804,34 +841,33 @@ int launch_batch_t(char *bws, const BatchLayout &BL, int64_t n_items, bool diag,
     rc = cuda_status(cudaMemsetAsync(&hdr->cursor, 0, sizeof(hdr->cursor), stream),
                      "batch cursor reset");
     if (rc) return rc;
-    k<<<(unsigned)grid, A * B, SM::bytes, stream>>>(
+    k<<<(unsigned)grid, Cfg::THREADS, Cfg::smem_bytes, stream>>>(
         reinterpret_cast<const BatchScene *>(bws + BL.scenes),
         reinterpret_cast<const int2 *>(bws + BL.items), n_items, &hdr->cursor,
         reinterpret_cast<unsigned long long *>(counters), &hdr->status);
     return cuda_status(cudaGetLastError(), "focus_batch_staged launch");
 }
 
-
-
-// Per-chunk-size dispatch over the (tile, window) variants; instantiated in
-// staged_c32.cu / staged_c64.cu / staged_c128.cu.  SARBP_EINVAL (with a
-// message) for a variant that is not built.
-#define SARBP_STAGED_TILES(X, C) \
-    X(C, 16, 16, 128) X(C, 16, 16, 160) X(C, 16, 8, 128) X(C, 32, 8, 128) X(C, 64, 4, 128)
+// Per-chunk-size dispatch over the (tile, window, stage) variants;
+// instantiated in staged_c32.cu / staged_c64.cu / staged_c128.cu.
+// SARBP_EINVAL (with a message) for a variant that is not built.
+#define SARBP_STAGED_TILES(X, C)                                                            \
+    X(C, 16, 16, 160, 32) X(C, 16, 16, 160, 16) X(C, 16, 16, 128, 32) X(C, 16, 8, 128, 32)   \
+    X(C, 16, 8, 128, 16) X(C, 32, 8, 128, 32) X(C, 64, 4, 128, 32)
 
 template <int C>
 int launch_staged_chunk(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L,
                         char *ws, bool queued, double *out, int32_t *nvalid, uint64_t *checksum,
                         uint64_t *counters, cudaStream_t stream)
 {
-#define X(C_, A, B, W)                                                                      \
-    if (T.tile0 == A && T.tile1 == B && T.window == W)                                      \
-        return launch_staged_t<C_, A, B, W>(P, L, ws, queued, out, nvalid, checksum,        \
-                                            counters, stream);
+#define X(C_, A, B, W, S)                                                                   \
+    if (T.tile0 == A && T.tile1 == B && T.window == W && T.stage == S)                      \
+        return launch_staged_t<StagedCfg<C_, A, B, W, S>>(P, L, ws, queued, out, nvalid,    \
+                                                          checksum, counters, stream);
     SARBP_STAGED_TILES(X, C)
 #undef X
-    set_error("staged path: unsupported tuning chunk=%d tile=%dx%d window=%d", T.chunk, T.tile0,
-              T.tile1, T.window);
+    set_error("staged path: unsupported tuning chunk=%d tile=%dx%d window=%d stage=%d", T.chunk,
+              T.tile0, T.tile1, T.window, T.stage);
     return SARBP_EINVAL;
 }
 
@@ -839,13 +875,14 @@ template <int C>
 int launch_batch_chunk(char *bws, const BatchLayout &BL, const sarbp_tuning &T, int64_t n_items,
                        bool diag, uint64_t *counters, cudaStream_t stream)
 {
-#define X(C_, A, B, W)                                                                      \
-    if (T.tile0 == A && T.tile1 == B && T.window == W)                                      \
-        return launch_batch_t<C_, A, B, W>(bws, BL, n_items, diag, counters, stream);
+#define X(C_, A, B, W, S)                                                                   \
+    if (T.tile0 == A && T.tile1 == B && T.window == W && T.stage == S)                      \
+        return launch_batch_t<StagedCfg<C_, A, B, W, S>>(bws, BL, n_items, diag, counters,  \
+                                                         stream);
     SARBP_STAGED_TILES(X, C)
 #undef X
-    set_error("batch path: unsupported tuning chunk=%d tile=%dx%d window=%d", T.chunk, T.tile0,
-              T.tile1, T.window);
+    set_error("batch path: unsupported tuning chunk=%d tile=%dx%d window=%d stage=%d", T.chunk,
+              T.tile0, T.tile1, T.window, T.stage);
     return SARBP_EINVAL;
 }
 

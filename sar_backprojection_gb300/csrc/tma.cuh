@@ -55,6 +55,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32
     return false;
 }
 
+// Orders this thread's earlier generic-proxy shared-memory accesses (and
+// those it has observed) before its later async-proxy (TMA) accesses.
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 // 2-D tiled TMA load of one box into shared memory, completion counted on bar.
 // x (innermost coordinate) times the element size must be a multiple of 16 B.
 __device__ __forceinline__ void tma_load_2d(void *dst, const void *tensor_map, uint64_t *bar,
