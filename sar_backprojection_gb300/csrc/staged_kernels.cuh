@@ -49,6 +49,7 @@ namespace sarbp {
 
 constexpr int kMaxPassStages = 128;        // stages whose windows are kept at once
 constexpr int kMaxBuf = 4;                 // ring buffers (64 pulses / 16-pulse stages)
+constexpr int kMaxTileThreads = 256;       // pixels (threads) per tile
 constexpr uint32_t kWaitLimit = 1u << 22;  // mbarrier polls before giving up
 
 // Compile-time shape of a staged variant.
@@ -66,7 +67,31 @@ struct StagedCfg {
     static_assert(NBUF <= kMaxBuf && (NBUF & (NBUF - 1)) == 0, "ring");
     static_assert(CHUNK % STAGE == 0 && kMaxPassStages % R == 0, "chunk");
     static_assert(buf_bytes % 128 == 0, "TMA destinations stay 128-byte aligned");
+    static_assert(THREADS <= kMaxTileThreads && (THREADS & (THREADS - 1)) == 0, "tile");
 };
+
+// Ascending bitonic sort of N keys in shared memory, one key per thread of
+// the CTA (N = blockDim.x, a power of two); keys must be in place and
+// visible (after a barrier) on entry.
+template <int N>
+__device__ __forceinline__ void cta_bitonic_sort(unsigned long long *a, int t)
+{
+#pragma unroll 1
+    for (int k = 2; k <= N; k <<= 1) {
+#pragma unroll 1
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const int p = t ^ j;
+            if (p > t) {
+                const unsigned long long x = a[t], y = a[p];
+                if ((x > y) == ((t & k) == 0)) {
+                    a[t] = y;
+                    a[p] = x;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
 
 template <int T0, int T1>
 __device__ __forceinline__ void staged_tile_pixel(int t, int64_t tile0, int64_t tile1,
@@ -136,6 +161,7 @@ struct StagedShared {
     int issued[kMaxBuf];              // a copy was ever issued into the buffer
     int stop;                         // a bounded wait gave up
     int wlo[kMaxPassStages], whi[kMaxPassStages];   // range windows of a pass
+    unsigned long long lane_key[kMaxTileThreads];   // lane assignment sort
     long long lo, hi;                 // tile-wide pulse range
     long long item[2];                // persistent kernels: current work item
 };
@@ -192,11 +218,29 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
     const int t = threadIdx.x, lane = t & 31;
     int64_t i0, i1;
     staged_tile_pixel<Cfg::T0, Cfg::T1>(t, tile0, tile1, i0, i1);
-    const bool inside = i0 < P.dim0 && i1 < P.dim1;
-    const int64_t ii = inside ? i0 + P.dim0 * i1 : 0;
+    bool inside = i0 < P.dim0 && i1 < P.dim1;
+    int64_t ii = inside ? i0 + P.dim0 * i1 : 0;
     int64_t lo = 0, hi = -1;
-    const bool active =
+    bool active =
         inside && pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi);
+
+    // ---- lane assignment: the tile's pixels in order of aperture midpoint.
+    // Pixels without an aperture (masked, outside the DEM) gather in the last
+    // warps, which then skip every stage, and each warp's apertures start and
+    // end close together, so more of its stages take the fast path.
+    sh.lane_key[t] = ((unsigned long long)(active ? (uint32_t)(lo + hi) : 0xffffffffu) << 16) |
+                     (unsigned)t;
+    __syncthreads();
+    cta_bitonic_sort<Cfg::THREADS>(sh.lane_key, t);
+    {
+        const int src = (int)(sh.lane_key[t] & 0xffffu);
+        staged_tile_pixel<Cfg::T0, Cfg::T1>(src, tile0, tile1, i0, i1);
+        inside = i0 < P.dim0 && i1 < P.dim1;
+        ii = inside ? i0 + P.dim0 * i1 : 0;
+        lo = 0;
+        hi = -1;
+        active = inside && pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi);
+    }
 
     if (t == 0) {
         sh.lo = LLONG_MAX;
@@ -369,7 +413,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                     if (fast) {
                         // two pulses per f32x2 instruction, the scalar path's
                         // operation sequence per pulse (bit-identical values)
-                        valid_mask = 0xffffffffu;
+                        valid_mask = STAGE == 32 ? 0xffffffffu : (1u << STAGE) - 1u;
                         const f2_t mx2 = f2_dup(S.mx), my2 = f2_dup(S.my), mz2 = f2_dup(S.mz);
                         const f2_t c1_2 = f2_dup(S.c1), c2_2 = f2_dup(S.c2), c3_2 = f2_dup(S.c3);
                         const f2_t g0_2 = f2_dup(S.g0), a_2 = f2_dup(S.a), r0sq2 = f2_dup(S.r0sq);
