@@ -93,6 +93,14 @@ bool build_params(const sarbp_scene *s, SceneParams *p)
     p->beta_f = (float)p->beta;
     p->beta2_f = (float)(2.0 * p->beta);
     p->inv_dra_f = (float)p->inv_dra;
+    auto dup = [](float v) {
+        uint32_t b;
+        memcpy(&b, &v, sizeof(b));
+        return ((unsigned long long)b << 32) | b;
+    };
+    p->inv_dra_f2 = dup(p->inv_dra_f);
+    p->beta_f2 = dup(p->beta_f);
+    p->magic_f2 = dup(12582912.0f);   // 1.5 * 2^23: x + magic rounds x to an integer
     return true;
 }
 

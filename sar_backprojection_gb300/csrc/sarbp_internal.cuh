@@ -34,6 +34,8 @@ struct SceneParams {
     float k1_hi, k1_lo;      // k4pl/(2*pi), turns per metre
     float k2_hi, k2_lo;      // beta/(2*pi), turns per square metre
     float k4pl_f, beta_f, beta2_f, inv_dra_f;
+    // the same FP32 values in both halves of a packed f32x2 operand
+    unsigned long long inv_dra_f2, beta_f2, magic_f2;
 };
 
 // Aperture of one pixel, clamped to the kept pulses 0 < a < naz-1

@@ -103,15 +103,35 @@ __device__ __forceinline__ void staged_tile_pixel(int t, int64_t tile0, int64_t 
     i1 = tile1 * T1 + (w / (T0 / 8)) * 4 + (lane >> 3);
 }
 
+// The per-pulse coefficients of a chunk setup, each in both halves of an
+// f32x2 pair: the operands of the fast path, and (low half) of the scalar
+// paths, so only one copy stays live across a chunk's stages.
+struct StageCoef {
+    f2_t mx, my, mz, c1, c2, c3, g0, a, r0sq;
+};
+
+__device__ __forceinline__ float f2_lo(f2_t v)
+{
+    float lo, hi;
+    f2_unpack(v, lo, hi);
+    return lo;
+}
+
+__device__ __forceinline__ StageCoef stage_coef(const ChunkSetup &S)
+{
+    return StageCoef{f2_dup(S.mx), f2_dup(S.my), f2_dup(S.mz), f2_dup(S.c1),  f2_dup(S.c2),
+                     f2_dup(S.c3), f2_dup(S.g0), f2_dup(S.a),  f2_dup(S.r0sq)};
+}
+
 // FP32 per-pulse range geometry: D = R^2 - R0^2, dR = R - R0, the window
 // column of the FP32 range bin, and whether that bin is within the tie band.
-__device__ __forceinline__ void pulse_eval(const ChunkSetup &S, float4 e, float inv_dra,
+__device__ __forceinline__ void pulse_eval(const StageCoef &S, float4 e, float inv_dra,
                                            int colbias, float tie, float &D, float &dR,
                                            int &col, bool &amb)
 {
-    D = fmaf(S.mx, e.x, fmaf(S.my, e.y, fmaf(S.mz, e.z, e.w)));
-    dR = D * fmaf(fmaf(S.c3, D, S.c2), D, S.c1);
-    const float g = fmaf(dR, inv_dra, S.g0);
+    D = fmaf(f2_lo(S.mx), e.x, fmaf(f2_lo(S.my), e.y, fmaf(f2_lo(S.mz), e.z, e.w)));
+    dR = D * fmaf(fmaf(f2_lo(S.c3), D, f2_lo(S.c2)), D, f2_lo(S.c1));
+    const float g = fmaf(dR, inv_dra, f2_lo(S.g0));
     const float t = __fadd_rn(g, 12582912.0f);
     col = __float_as_int(t) + colbias;
     amb = fabsf(__fsub_rn(g, __fsub_rn(t, 12582912.0f))) > tie;
@@ -125,13 +145,13 @@ __device__ __forceinline__ float4 stage_e(const float4 *stab, int j)
 }
 
 // R^2 * exp(-j*dphi) as (wc, ws): term = (vx + j*vy) * (wc - j*ws).
-__device__ __forceinline__ void pulse_phasor(const ChunkSetup &S, float D, float dR, float beta,
+__device__ __forceinline__ void pulse_phasor(const StageCoef &S, float D, float dR, float beta,
                                              float &wc, float &ws)
 {
-    const float ph = dR * fmaf(beta, dR, S.a);
+    const float ph = dR * fmaf(beta, dR, f2_lo(S.a));
     float sn, cn;
     __sincosf(ph, &sn, &cn);
-    const float w = S.r0sq + D;
+    const float w = f2_lo(S.r0sq) + D;
     wc = w * cn;
     ws = w * sn;
 }
@@ -265,6 +285,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
     bool stopped = false;
     ChunkSetup S;
     safe_setup(S, 0);
+    StageCoef C = stage_coef(S);
     bool gwork = false;                   // pixel has pulses in the current chunk
     int64_t cur_chunk = -1;
     float gre = 0.f, gim = 0.f;           // FP32 partial sum of the current chunk
@@ -363,6 +384,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                     } else {
                         safe_setup(S, 0);
                     }
+                    C = stage_coef(S);
                 }
                 const bool ready = mbar_wait(&sh.full_bar[b], use & 1, kWaitLimit);
                 if (!ready) *(volatile int *)&sh.stop = 1;
@@ -414,11 +436,10 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                         // two pulses per f32x2 instruction, the scalar path's
                         // operation sequence per pulse (bit-identical values)
                         valid_mask = STAGE == 32 ? 0xffffffffu : (1u << STAGE) - 1u;
-                        const f2_t mx2 = f2_dup(S.mx), my2 = f2_dup(S.my), mz2 = f2_dup(S.mz);
-                        const f2_t c1_2 = f2_dup(S.c1), c2_2 = f2_dup(S.c2), c3_2 = f2_dup(S.c3);
-                        const f2_t g0_2 = f2_dup(S.g0), a_2 = f2_dup(S.a), r0sq2 = f2_dup(S.r0sq);
-                        const f2_t idra2 = f2_dup(P.inv_dra_f), beta2 = f2_dup(P.beta_f);
-                        const f2_t magic2 = f2_dup(12582912.0f);
+                        const f2_t mx2 = C.mx, my2 = C.my, mz2 = C.mz;
+                        const f2_t c1_2 = C.c1, c2_2 = C.c2, c3_2 = C.c3;
+                        const f2_t g0_2 = C.g0, a_2 = C.a, r0sq2 = C.r0sq;
+                        const f2_t idra2 = P.inv_dra_f2, beta2 = P.beta_f2, magic2 = P.magic_f2;
                         const ulonglong2 *sp = reinterpret_cast<const ulonglong2 *>(stab);
                         float rmax = 0.f;     // largest |g - rint(g)|: a tie test per stage
 #pragma unroll
@@ -467,7 +488,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                                 float D, dR;
                                 int col;
                                 bool amb;
-                                pulse_eval(S, stage_e(stab, j), P.inv_dra_f, colbias, tie, D, dR,
+                                pulse_eval(C, stage_e(stab, j), P.inv_dra_f, colbias, tie, D, dR,
                                            col, amb);
                                 if (amb) amb_mask |= 1u << j;
                             }
@@ -483,7 +504,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                             float D, dR;
                             int col;
                             bool amb;
-                            pulse_eval(S, stage_e(stab, j), P.inv_dra_f, colbias, tie, D, dR, col, amb);
+                            pulse_eval(C, stage_e(stab, j), P.inv_dra_f, colbias, tie, D, dR, col, amb);
                             const bool inap = (apmask >> j) & 1u;
                             const int bin = col + b0;
                             const bool ok = inap && (unsigned)bin < nra_m1;
@@ -494,7 +515,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                             if (ok && !inw) miss_mask |= 1u << j;
                             if (inap && amb) amb_mask |= 1u << j;
                             float wc, ws;
-                            pulse_phasor(S, D, dR, P.beta_f, wc, ws);
+                            pulse_phasor(C, D, dR, P.beta_f, wc, ws);
                             sre = fmaf(v.x, wc, fmaf(v.y, ws, sre));
                             sim = fmaf(v.y, wc, fmaf(-v.x, ws, sim));
                             if (kChecksum && ok) cs += mix64(K + j, bin);
@@ -510,7 +531,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                             float D, dR;
                             int col;
                             bool amb;
-                            pulse_eval(S, stage_e(stab, j), P.inv_dra_f, colbias, tie, D, dR, col, amb);
+                            pulse_eval(C, stage_e(stab, j), P.inv_dra_f, colbias, tie, D, dR, col, amb);
                             int bin_old = col + b0;
                             bool ok_old;
                             float2 v_old = make_float2(0.f, 0.f);
@@ -540,7 +561,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                                 }
                             }
                             float wc, ws;
-                            pulse_phasor(S, D, dR, P.beta_f, wc, ws);
+                            pulse_phasor(C, D, dR, P.beta_f, wc, ws);
                             const float dx = v_new.x - v_old.x, dy = v_new.y - v_old.y;
                             sre = fmaf(dx, wc, fmaf(dy, ws, sre));
                             sim = fmaf(dy, wc, fmaf(-dx, ws, sim));
