@@ -181,6 +181,8 @@ struct StagedShared {
     int issued[kMaxBuf];              // a copy was ever issued into the buffer
     int stop;                         // a bounded wait gave up
     int wlo[kMaxPassStages], whi[kMaxPassStages];   // range windows of a pass
+    float4 geo[kMaxPassStages][2];    // per stage: first pulse t(K) (hi parts) and
+                                      // s = t(K+STAGE-1) - t(K); 1/|s|^2, chord deviation
     unsigned long long lane_key[kMaxTileThreads];   // lane assignment sort
     long long lo, hi;                 // tile-wide pulse range
     long long item[2];                // persistent kernels: current work item
@@ -294,42 +296,44 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
         for (int64_t cb = c_first; cb <= c_last && !stopped; cb += kMaxPassStages) {
             const int npass = (int)min((int64_t)kMaxPassStages, c_last - cb + 1);
             // ---- window prologue: bins every pixel can reach per stage ----
+            // stage geometry of the pass into shared memory (one stage per thread)
             for (int q = t; q < npass; q += blockDim.x) {
+                const int64_t K = (cb + q) * STAGE;
+                const int64_t kb = min(K + STAGE - 1, P.naz - 1);
+                const float4 ta = __ldg(&pff[K].hi), tb = __ldg(&pff[kb].hi);
+                const float sx = tb.x - ta.x, sy = tb.y - ta.y, sz = tb.z - ta.z;
+                const float ss = sx * sx + sy * sy + sz * sz;
+                sh.geo[q][0] = make_float4(ta.x, ta.y, ta.z, ss > 0.f ? 1.0f / ss : 0.f);
+                sh.geo[q][1] = make_float4(sx, sy, sz, __ldg(&sdev[cb + q]));
                 sh.wlo[q] = INT_MAX;
                 sh.whi[q] = INT_MIN;
             }
             __syncthreads();
+#pragma unroll 2
             for (int q = 0; q < npass; ++q) {
                 const int64_t K = (cb + q) * STAGE;
                 int blo = INT_MAX, bhi = INT_MIN;
                 if (active && lo <= K + STAGE - 1 && hi >= K) {
-                    const int64_t ka = K, kb = min(K + STAGE - 1, P.naz - 1);
-                    const float4 ta = __ldg(&pff[ka].hi), tb = __ldg(&pff[kb].hi);
-                    const float dev = __ldg(&sdev[cb + q]);
-                    const float ax = pf.xh - ta.x, ay = pf.yh - ta.y, az = pf.zh - ta.z;
-                    const float bx = pf.xh - tb.x, by = pf.yh - tb.y, bz = pf.zh - tb.z;
-                    // approximate square roots and quotient (relative error
-                    // ~1e-6, ~4 mm at 4 km): the window keeps a 1-bin margin
+                    // distances from the pixel to the stage's pulse segment:
+                    // endpoints (max), closest point (min), widened by the
+                    // chord deviation; approximate square roots (relative
+                    // error ~1e-6, ~4 mm at 4 km) inside the 1-bin margin
+                    const float4 g0 = sh.geo[q][0], g1 = sh.geo[q][1];
+                    const float ax = pf.xh - g0.x, ay = pf.yh - g0.y, az = pf.zh - g0.z;
                     const float a2 = ax * ax + ay * ay + az * az;
+                    const float d = ax * g1.x + ay * g1.y + az * g1.z;
+                    const float u = d * g0.w;
+                    const float bx = ax - g1.x, by = ay - g1.y, bz = az - g1.z;
                     const float b2 = bx * bx + by * by + bz * bz;
-                    const float ra = a2 > 0.f ? a2 * rsqrtf(a2) : 0.f;
-                    const float rb = b2 > 0.f ? b2 * rsqrtf(b2) : 0.f;
-                    const float sx = tb.x - ta.x, sy = tb.y - ta.y, sz = tb.z - ta.z;
-                    const float ss = sx * sx + sy * sy + sz * sz;
-                    float u = ss > 0.f ? __fdividef(ax * sx + ay * sy + az * sz, ss) : 0.f;
-                    u = fminf(fmaxf(u, 0.f), 1.f);
-                    const float cx = ax - u * sx, cy = ay - u * sy, cz = az - u * sz;
-                    const float c2 = cx * cx + cy * cy + cz * cz;
-                    const float rc = c2 > 0.f ? c2 * rsqrtf(c2) : 0.f;
-                    const float rmin = fminf(fminf(ra, rb), rc) - dev;
-                    const float rmax = fmaxf(ra, rb) + dev;
-                    blo = (int)floorf((rmin - P.near_hi) * P.inv_dra_f) - 1;
-                    bhi = (int)ceilf((rmax - P.near_hi) * P.inv_dra_f) + 1;
+                    const float rmin2 = (u > 0.f && u < 1.f) ? fmaf(-d, u, a2) : fminf(a2, b2);
+                    const float rmax2 = fmaxf(a2, b2);
+                    const float rmin = rmin2 > 0.f ? rmin2 * rsqrtf(rmin2) : 0.f;
+                    const float rmax = rmax2 > 0.f ? rmax2 * rsqrtf(rmax2) : 0.f;
+                    blo = (int)floorf((rmin - g1.w - P.near_hi) * P.inv_dra_f) - 1;
+                    bhi = (int)ceilf((rmax + g1.w - P.near_hi) * P.inv_dra_f) + 1;
                 }
-                for (int o = 16; o > 0; o >>= 1) {
-                    blo = min(blo, __shfl_xor_sync(0xffffffffu, blo, o));
-                    bhi = max(bhi, __shfl_xor_sync(0xffffffffu, bhi, o));
-                }
+                blo = __reduce_min_sync(0xffffffffu, blo);
+                bhi = __reduce_max_sync(0xffffffffu, bhi);
                 if (lane == 0 && blo <= bhi) {
                     atomicMin(&sh.wlo[q], blo);
                     atomicMax(&sh.whi[q], bhi);
@@ -352,6 +356,9 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                 tma_load_2d(base, raw_map, &sh.full_bar[b], window_start(q), (int)K);
                 bulk_load(base + Cfg::raw_bytes, ptab + K, (uint32_t)Cfg::tab_bytes,
                           &sh.full_bar[b]);
+                // the stage loaded NBUF stages from now: into L2 meanwhile
+                if (q + NBUF < npass)
+                    tma_prefetch_2d(raw_map, window_start(q + NBUF), (int)(K + NBUF * STAGE));
                 sh.last_parity[b] = use & 1;
                 sh.issued[b] = 1;
             };
@@ -743,7 +750,7 @@ focus_mixed_staged_queue_kernel(const SceneParams P, const __grid_constant__ CUt
 template <class Cfg>
 constexpr int staged_min_blocks()
 {
-    return Cfg::smem_bytes * 3 + 3 * 1024 <= 227 * 1024 ? 3 : 2;
+    return (Cfg::smem_bytes + sizeof(StagedShared) + 1024) * 3 <= 228 * 1024 ? 3 : 2;
 }
 
 // Many scenes in one persistent launch: CTAs pull (scene, tile) work items
