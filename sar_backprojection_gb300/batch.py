@@ -26,11 +26,12 @@ from . import _lib
 from .focuser import resolve_tuning
 from .scene import DeviceScene
 
-# (tile0, tile1, window) variants of the staged kernel
-STAGED_TILINGS = ((16, 16, 128), (16, 16, 160), (16, 8, 128), (32, 8, 128), (64, 4, 128))
+# (tile0, tile1, window, chunk) variants of the staged kernel the autotuner times
+STAGED_TILINGS = ((16, 16, 160, 64), (16, 16, 160, 128), (16, 16, 128, 64), (16, 8, 128, 64),
+                  (16, 8, 128, 128), (32, 8, 128, 64))
 
 
-def staged_tuning(tile0: int = 16, tile1: int = 16, window: int = 160, chunk: int = 32,
+def staged_tuning(tile0: int = 16, tile1: int = 16, window: int = 160, chunk: int = 64,
                   stage: int = 32) -> _lib.Tuning:
     return resolve_tuning({"chunk": chunk, "tile0": tile0, "tile1": tile1, "staged": 1,
                            "window": window, "stage": stage})
@@ -189,7 +190,7 @@ class Autotuner:
     def __init__(self, candidates=STAGED_TILINGS, repeats: int = 3):
         self.candidates = candidates
         self.repeats = repeats
-        self.cache: dict[tuple, tuple[int, int]] = {}
+        self.cache: dict[tuple, tuple] = {}
         self.timings: dict[tuple, dict] = {}
 
     @staticmethod
@@ -203,8 +204,8 @@ class Autotuner:
         key = self.signature(scenes)
         if key not in self.cache:
             best, times = None, {}
-            for t0, t1, w in self.candidates:
-                bf = BatchFocuser(scenes, staged_tuning(t0, t1, w), graph=False)
+            for cand in self.candidates:
+                bf = BatchFocuser(scenes, staged_tuning(*cand), graph=False)
                 bf.run()
                 torch.cuda.synchronize(bf.device)
                 a = torch.cuda.Event(enable_timing=True)
@@ -215,9 +216,9 @@ class Autotuner:
                 b.record()
                 torch.cuda.synchronize(bf.device)
                 ms = a.elapsed_time(b) / self.repeats
-                times[f"{t0}x{t1}/{w}"] = ms
+                times["{}x{}/{}/c{}".format(*cand)] = ms
                 if best is None or ms < best[0]:
-                    best = (ms, (t0, t1, w))
+                    best = (ms, cand)
                 del bf
             self.cache[key] = best[1]
             self.timings[key] = times

@@ -104,15 +104,17 @@ bool build_params(const sarbp_scene *s, SceneParams *p)
     return true;
 }
 
-// Library default: the TMA-staged kernel with one CTA per tile, 32-pulse
-// chunks, 16 x 16 pixel tiles with a 160-bin window (fastest measured on the
-// 4000 x 250 / 40001-pulse workload: 464 Gpix-pulse/s against 427 for the
-// cost-ordered tile queue, whose order scatters neighbouring tiles in time
-// and so loses the L2 reuse of their shared raw windows).
+// Library default: the TMA-staged kernel with one CTA per tile, 64-pulse
+// chunks (one float-float reference per 64 pulses), 32-pulse stages, 16 x 16
+// pixel tiles with a 160-bin window.  On the 4000 x 250 / 40001-pulse
+// workload 128-pulse chunks measure 2 % faster, but halve the pulse spacing
+// at which the FP32 series gives way to the FP64 body; the cost-ordered tile
+// queue (staged=2) measured slower, its order scattering neighbouring tiles
+// in time and so losing the L2 reuse of their shared raw windows.
 bool valid_tuning(sarbp_tuning *t)
 {
     if (t->chunk == 0 && t->tile0 == 0 && t->tile1 == 0 && t->staged == 0) {
-        t->chunk = 32;
+        t->chunk = 64;
         t->tile0 = 16;
         t->tile1 = 16;
         t->staged = 1;

@@ -26,7 +26,8 @@ def scenes():
     return out
 
 
-@pytest.mark.parametrize("tiling", batch.STAGED_TILINGS, ids=lambda t: f"{t[0]}x{t[1]}w{t[2]}")
+@pytest.mark.parametrize("tiling", batch.STAGED_TILINGS,
+                         ids=lambda t: f"{t[0]}x{t[1]}w{t[2]}c{t[3]}")
 @pytest.mark.parametrize("graph", [False, True], ids=["direct", "graph"])
 def test_batch_equals_single_scene(scenes, tiling, graph):
     tuning = batch.staged_tuning(*tiling)
@@ -58,6 +59,6 @@ def test_batch_quality_against_fp64(scenes):
 def test_autotuner_picks_a_candidate(scenes):
     at = batch.Autotuner(repeats=1)
     t = at.pick(scenes[:3])
-    assert (t.tile0, t.tile1, t.window) in batch.STAGED_TILINGS and t.staged == 1
+    assert (t.tile0, t.tile1, t.window, t.chunk) in batch.STAGED_TILINGS and t.staged == 1
     assert at.pick(scenes[:3]).tile0 == t.tile0        # cached
     assert len(at.timings) == 1
