@@ -92,7 +92,12 @@ typedef struct sarbp_tuning {
                              tile queue */
     int32_t window;       /* staged: range bins staged per pulse stage (0: default) */
     int32_t stage;        /* staged: pulses per TMA stage, 16 or 32 (0: default)   */
-    int32_t reserved[2];
+    int32_t wait_polls;   /* staged, diagnostic: mbarrier polls before a stage wait
+                             gives up (0: default 2^22) */
+    int32_t withhold;     /* staged, diagnostic: 1 never issues the first stage's
+                             copies of each pass, so that stage's wait runs out
+                             (exercises the timeout path, see sarbp_mixed_status);
+                             0 in normal use */
 } sarbp_tuning;
 
 /* Device counters written by the mixed kernel when `counters` is non-NULL. */
@@ -171,6 +176,16 @@ SARBP_API int sarbp_focus_mixed_prepared(const sarbp_scene *scene, const sarbp_t
                                          double *out, int32_t *nvalid, uint64_t *checksum,
                                          uint64_t *counters, void *workspace,
                                          size_t workspace_bytes, void *stream);
+
+/*
+ * Status of the mixed-path kernels that ran on `workspace` since it was last
+ * prepared or queried: SARBP_ETIMEOUT when a bounded device wait gave up
+ * (the kernel then stopped early, its image is incomplete, and the context
+ * stays usable), SARBP_OK otherwise.  Synchronises `stream`, then clears the
+ * status.  No counterpart in the reference (its kernels have no device-side
+ * waits).
+ */
+SARBP_API int sarbp_mixed_status(void *workspace, size_t workspace_bytes, void *stream);
 
 /*
  * Batches: many scenes of uneven size in one persistent launch.

@@ -53,7 +53,7 @@ class Tuning(C.Structure):
     _fields_ = [
         ("chunk", C.c_int32), ("tile0", C.c_int32), ("tile1", C.c_int32),
         ("staged", C.c_int32), ("window", C.c_int32), ("stage", C.c_int32),
-        ("reserved", C.c_int32 * 2),
+        ("wait_polls", C.c_int32), ("withhold", C.c_int32),
     ]
 
     def as_dict(self) -> dict:
@@ -75,6 +75,7 @@ SIGNATURES = {
     "sarbp_focus_mixed_prepared": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, _P, _P,
                                              _P, _P, C.c_size_t, _P]),
     "sarbp_probe_issue_rates": (C.c_int, [C.POINTER(C.c_double), _P]),
+    "sarbp_mixed_status": (C.c_int, [_P, C.c_size_t, _P]),
     "sarbp_focus_mixed_noalloc": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, _P, _P,
                                             _P, _P]),
     "sarbp_tile_count": (C.c_int64, [C.POINTER(Scene), C.POINTER(Tuning)]),

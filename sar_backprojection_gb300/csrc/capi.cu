@@ -101,6 +101,8 @@ bool build_params(const sarbp_scene *s, SceneParams *p)
     p->inv_dra_f2 = dup(p->inv_dra_f);
     p->beta_f2 = dup(p->beta_f);
     p->magic_f2 = dup(12582912.0f);   // 1.5 * 2^23: x + magic rounds x to an integer
+    p->wait_polls = 1u << 22;         // staged kernels: set per launch from the tuning
+    p->withhold = 0;
     return true;
 }
 
@@ -127,6 +129,14 @@ bool valid_tuning(sarbp_tuning *t)
     }
     if (t->staged && t->window == 0) t->window = (t->tile0 * t->tile1 >= 256) ? 160 : 128;
     if (t->stage == 0) t->stage = 32;
+    if (t->wait_polls < 0) {
+        set_error("tuning.wait_polls must be >= 0 (got %d)", t->wait_polls);
+        return false;
+    }
+    if (t->withhold != 0 && t->withhold != 1) {
+        set_error("tuning.withhold must be 0 or 1 (got %d)", t->withhold);
+        return false;
+    }
     if (t->stage != 16 && t->stage != 32) {
         set_error("tuning.stage must be 16 or 32 (got %d)", t->stage);
         return false;
@@ -243,6 +253,27 @@ SARBP_API int sarbp_focus_mixed(const sarbp_scene *scene, const sarbp_tuning *tu
     if (rc) return rc;
     return launch_mixed_main(P, T, workspace, workspace_bytes, out, nvalid, checksum, counters,
                              s);
+}
+
+SARBP_API int sarbp_mixed_status(void *workspace, size_t workspace_bytes, void *stream)
+{
+    if (!workspace || workspace_bytes < sizeof(StatusBlock)) {
+        set_error("sarbp_mixed_status: workspace missing or too small");
+        return SARBP_EWORKSPACE;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    StatusBlock st;
+    int rc = cuda_status(cudaMemcpyAsync(&st, workspace, sizeof(st), cudaMemcpyDeviceToHost, s),
+                         "sarbp_mixed_status: read");
+    if (rc) return rc;
+    rc = cuda_status(cudaStreamSynchronize(s), "sarbp_mixed_status: synchronize");
+    if (rc) return rc;
+    if (!st.error) return SARBP_OK;
+    rc = cuda_status(cudaMemsetAsync(workspace, 0, sizeof(StatusBlock), s), "sarbp_mixed_status: clear");
+    if (rc) return rc;
+    set_error("mixed kernel: a bounded device wait gave up (site %u); the image is incomplete",
+              st.where);
+    return SARBP_ETIMEOUT;
 }
 
 SARBP_API int64_t sarbp_tile_count(const sarbp_scene *scene, const sarbp_tuning *tuning)

@@ -368,6 +368,10 @@ int launch_mixed_prepare(const SceneParams &P, const sarbp_tuning &T, void *work
     if (rc) return rc;
     char *ws = static_cast<char *>(workspace);
     // the staged kernels read the pair-interleaved table (f32x2 operands)
+    // a prepared workspace starts with a clear status (sarbp_mixed_status)
+    rc = cuda_status(cudaMemsetAsync(ws + L.status, 0, sizeof(StatusBlock), stream),
+                     "status reset");
+    if (rc) return rc;
     rc = launch_chunk_table(P, T.chunk, T.stage > 0 ? T.stage : 32, T.staged != 0, ws, L, stream);
     if (rc) return rc;
     // persistent staged path: tiles in decreasing estimated cost
@@ -388,8 +392,12 @@ int launch_mixed_main(const SceneParams &P, const sarbp_tuning &T, void *workspa
         return SARBP_ERANGE;
     }
     char *ws = static_cast<char *>(workspace);
-    if (T.staged)
-        return launch_staged(P, T, L, ws, T.staged == 2, out, nvalid, checksum, counters, stream);
+    if (T.staged) {
+        SceneParams Ps = P;
+        Ps.wait_polls = T.wait_polls > 0 ? (uint32_t)T.wait_polls : (1u << 22);
+        Ps.withhold = T.withhold;
+        return launch_staged(Ps, T, L, ws, T.staged == 2, out, nvalid, checksum, counters, stream);
+    }
     const int key = T.chunk * 1000000 + T.tile0 * 1000 + T.tile1;
     switch (key) {
         case 32 * 1000000 + 32 * 1000 + 8:

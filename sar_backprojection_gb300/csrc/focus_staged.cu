@@ -123,6 +123,8 @@ int batch_set_scene(void *bws, size_t bytes, int slot, int nscenes, const SceneP
     int rc = make_raw_map(P, T.window, T.stage, &B.map);
     if (rc) return rc;
     B.P = P;
+    B.P.wait_polls = T.wait_polls > 0 ? (uint32_t)T.wait_polls : (1u << 22);
+    B.P.withhold = T.withhold;
     B.tables = tables_of(static_cast<char *>(scene_ws), L);
     B.outputs = TileOutputs{reinterpret_cast<double2 *>(out), nvalid, checksum};
     rc = tiling_tiles(P, T, &B.ntile0, &B.ntiles);

@@ -36,6 +36,8 @@ struct SceneParams {
     float k4pl_f, beta_f, beta2_f, inv_dra_f;
     // the same FP32 values in both halves of a packed f32x2 operand
     unsigned long long inv_dra_f2, beta_f2, magic_f2;
+    uint32_t wait_polls;     // staged kernels: polls before a stage wait gives up
+    int32_t withhold;        // staged kernels, diagnostic: skip each pass's first copy
 };
 
 // Aperture of one pixel, clamped to the kept pulses 0 < a < naz-1

@@ -363,9 +363,10 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                 sh.issued[b] = 1;
             };
             const uint32_t it0 = cta.it;
-            // every buffer is free at a pass start: prime the ring
+            // every buffer is free at a pass start: prime the ring (a
+            // diagnostic withhold leaves stage 0 uncopied: its wait runs out)
             if (t == 0)
-                for (int q = 0; q < NBUF && q < npass; ++q)
+                for (int q = P.withhold ? 1 : 0; q < NBUF && q < npass; ++q)
                     issue(q, (int)((it0 + q) % NBUF), (it0 + q) / NBUF);
 
             for (int q = 0; q < npass; ++q) {
@@ -393,7 +394,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                     }
                     C = stage_coef(S);
                 }
-                const bool ready = mbar_wait(&sh.full_bar[b], use & 1, kWaitLimit);
+                const bool ready = mbar_wait(&sh.full_bar[b], use & 1, P.wait_polls);
                 if (!ready) *(volatile int *)&sh.stop = 1;
                 if (__any_sync(0xffffffffu, !ready) || *(volatile int *)&sh.stop) {
                     stopped = true;

@@ -35,6 +35,22 @@ class FocusResult:
     nvalid: torch.Tensor | None = None     # (npix,) int32 contributor counts
     checksum: torch.Tensor | None = None   # (npix,) int64 (bit pattern of uint64)
     counters: torch.Tensor | None = None   # (NUM_COUNTERS,) int64
+    workspace: torch.Tensor | None = None  # mixed: the workspace the kernels ran on
+
+    def status(self) -> int:
+        """Mixed path: SARBP_ETIMEOUT if a bounded device wait gave up (the image
+        is then incomplete), else SARBP_OK; synchronises the current stream and
+        clears the status.  Always SARBP_OK for the FP64 kernel."""
+        if self.workspace is None:
+            return _lib.SARBP_OK
+        return int(_lib.load().sarbp_mixed_status(self.workspace.data_ptr(),
+                                                  self.workspace.numel(),
+                                                  _stream_ptr(self.workspace.device)))
+
+    def check(self) -> "FocusResult":
+        """Raise SarbpError when status() is not SARBP_OK."""
+        _lib.check(self.status())
+        return self
 
     def to_numpy(self, dim0: int, dim1: int) -> np.ndarray:
         """complex128 image of shape (dim0, dim1), as the reference returns it."""
@@ -97,6 +113,7 @@ def focus(scene: DeviceScene, precision: str = "fp64", *, tuning=None,
         ctr_ptr = res.counters.data_ptr()
     _lib.check(lib.sarbp_focus_mixed(sc, C.byref(t), out.data_ptr(), nv_ptr, cs_ptr, ctr_ptr,
                                      workspace.data_ptr(), workspace.numel(), stream))
+    res.workspace = workspace
     return res
 
 
@@ -110,7 +127,9 @@ def FocalizzatoreBpPx(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
     scene = scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
                             near_range, dra, lambda_val, Sint, device=device)
     res = focus(scene, precision, tuning=tuning)
-    return res.to_numpy(scene.dim0, scene.dim1)
+    img = res.to_numpy(scene.dim0, scene.dim1)
+    res.check()          # a device wait that gave up leaves an incomplete image
+    return img
 
 
 def FocalizzatoreBpCuPy(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,

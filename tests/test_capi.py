@@ -100,5 +100,11 @@ def test_workspace_size_is_host_only():
     assert lib.sarbp_mixed_workspace_size(C.byref(s), C.byref(t)) == _lib.SARBP_EINVAL
     assert "staged" in _lib.last_error()
     t.staged = 1
+    t.withhold = 2                              # diagnostic field: 0 or 1
+    assert lib.sarbp_mixed_workspace_size(C.byref(s), C.byref(t)) == _lib.SARBP_EINVAL
+    t.withhold = 0
+    t.wait_polls = -1
+    assert lib.sarbp_mixed_workspace_size(C.byref(s), C.byref(t)) == _lib.SARBP_EINVAL
+    t.wait_polls = 0
     t.chunk = 48
     assert lib.sarbp_mixed_workspace_size(C.byref(s), C.byref(t)) == _lib.SARBP_EINVAL
