@@ -632,9 +632,11 @@ template <class Cfg>
 __device__ __forceinline__ StagedCta staged_cta_init(unsigned char *smem_dyn, StagedShared &sh)
 {
     StagedCta cta;
-    // TMA tile loads without swizzle need 128-byte aligned destinations
-    cta.smem = reinterpret_cast<unsigned char *>(
-        (reinterpret_cast<uintptr_t>(smem_dyn) + 127) & ~(uintptr_t)127);
+    // TMA tile loads need 128-byte aligned destinations.  The offset is
+    // applied as pointer arithmetic on the __shared__ array (no integer
+    // round trip), so the compiler keeps the shared address space and the
+    // stage reads compile to shared-memory loads.
+    cta.smem = smem_dyn + ((128u - (smem_addr(smem_dyn) & 127u)) & 127u);
     cta.sh = &sh;
     cta.it = 0;
     if (threadIdx.x == 0) {
