@@ -76,92 +76,80 @@ __device__ __forceinline__ void store_e(float4 *ptab, int64_t k, float4 e, bool 
     f[6] = e.w;
 }
 
-// Per-pulse tables and per-chunk references; one warp per chunk.
+// Per-pulse tables and per-chunk references: one CTA per chunk, one thread
+// per pulse (blockDim = chunk).
 __global__ void chunk_table_kernel(const SceneParams P, int chunk, int stage, int paired,
                                    float4 *__restrict__ ptab, PulseFF *__restrict__ pff,
                                    ChunkRef *__restrict__ ctab, float *__restrict__ sdev,
                                    int64_t nchunks)
 {
-    const int64_t c = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-    const int lane = threadIdx.x & 31;
+    __shared__ float4 s_max[4];
+    const int64_t c = blockIdx.x;
+    const int j = threadIdx.x, lane = j & 31;
     if (c >= nchunks) return;
     const int64_t k0 = chunk_ref(c, chunk, P.naz);
     const double x0 = P.tx[k0], y0 = P.ty[k0], z0 = P.tz[k0];
-    float mx = 0.f, my = 0.f, mz = 0.f, m2 = 0.f;
-    for (int j = lane; j < chunk; j += 32) {
-        const int64_t k = c * chunk + j;
-        if (k >= P.naz) {
-            // padding past the last pulse: copied with whole chunks by the
-            // staged kernel, must hold finite values (never a kept pulse)
-            store_e(ptab, k, make_float4(0.f, 0.f, 0.f, 0.f), paired);
-            continue;
-        }
+    const int64_t k = c * chunk + j;
+    float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (k < P.naz) {
         const double tx = P.tx[k], ty = P.ty[k], tz = P.tz[k];
         const double ex = tx - x0, ey = ty - y0, ez = tz - z0;
-        const double e2 = ex * ex + ey * ey + ez * ez;
-        const float4 e = make_float4((float)ex, (float)ey, (float)ez, (float)e2);
-        store_e(ptab, k, e, paired);
+        e = make_float4((float)ex, (float)ey, (float)ez, (float)(ex * ex + ey * ey + ez * ez));
         PulseFF f;
         split_ff(tx, f.hi.x, f.lo.x);
         split_ff(ty, f.hi.y, f.lo.y);
         split_ff(tz, f.hi.z, f.lo.z);
         f.hi.w = f.lo.w = 0.f;
         pff[k] = f;
-        // Bounds rounded up by one part in 2^20 so they hold for the FP32 values.
-        mx = fmaxf(mx, fabsf(e.x) * 1.000001f);
-        my = fmaxf(my, fabsf(e.y) * 1.000001f);
-        mz = fmaxf(mz, fabsf(e.z) * 1.000001f);
-        m2 = fmaxf(m2, e.w * 1.000001f);
     }
-    // Largest distance of the chunk's pulses from the chord between its first
-    // and last pulse (bounds the staged kernel's range windows).
-    const int64_t ka = c * chunk, kb = min(c * chunk + chunk - 1, P.naz - 1);
-    const double ax = P.tx[ka], ay = P.ty[ka], az = P.tz[ka];
-    const double sx = P.tx[kb] - ax, sy = P.ty[kb] - ay, sz = P.tz[kb] - az;
-    const double ss = sx * sx + sy * sy + sz * sz;
-    double dev = 0.0;
-    for (int64_t k = ka + lane; k <= kb; k += 32) {
-        const double qx = P.tx[k] - ax, qy = P.ty[k] - ay, qz = P.tz[k] - az;
-        const double u = ss > 0.0 ? (qx * sx + qy * sy + qz * sz) / ss : 0.0;
-        const double rx = qx - u * sx, ry = qy - u * sy, rz = qz - u * sz;
-        dev = fmax(dev, sqrt(rx * rx + ry * ry + rz * rz));
+    // padding past the last pulse is copied with whole stages by the staged
+    // kernels and must hold finite values (never a kept pulse)
+    store_e(ptab, k, e, paired);
+
+    // Largest distance of a stage's pulses from the chord between its first
+    // and last pulse (bounds the staged kernels' range windows); the stage's
+    // pulses are `stage` consecutive lanes of one warp.
+    const int64_t sa = c * chunk + (j / stage) * stage;
+    double sd = 0.0;
+    if (k < P.naz) {
+        const int64_t sb = min(sa + stage - 1, P.naz - 1);
+        const double bx = P.tx[sa], by = P.ty[sa], bz = P.tz[sa];
+        const double vx = P.tx[sb] - bx, vy = P.ty[sb] - by, vz = P.tz[sb] - bz;
+        const double vv = vx * vx + vy * vy + vz * vz;
+        const double qx = P.tx[k] - bx, qy = P.ty[k] - by, qz = P.tz[k] - bz;
+        const double u = vv > 0.0 ? (qx * vx + qy * vy + qz * vz) / vv : 0.0;
+        const double rx = qx - u * vx, ry = qy - u * vy, rz = qz - u * vz;
+        sd = sqrt(rx * rx + ry * ry + rz * rz);
     }
-    // The same per stage of `stage` pulses (the staged kernels' TMA unit):
-    // one pulse per lane.
-    for (int s = 0; s < chunk / stage; ++s) {
-        const int64_t sa = c * chunk + s * stage;
-        double sd = 0.0;
-        if (sa < P.naz) {
-            const int64_t sb = min(sa + stage - 1, P.naz - 1);
-            const double bx = P.tx[sa], by = P.ty[sa], bz = P.tz[sa];
-            const double vx = P.tx[sb] - bx, vy = P.ty[sb] - by, vz = P.tz[sb] - bz;
-            const double vv = vx * vx + vy * vy + vz * vz;
-            const int64_t k = sa + lane;
-            if (k <= sb) {
-                const double qx = P.tx[k] - bx, qy = P.ty[k] - by, qz = P.tz[k] - bz;
-                const double u = vv > 0.0 ? (qx * vx + qy * vy + qz * vz) / vv : 0.0;
-                const double rx = qx - u * vx, ry = qy - u * vy, rz = qz - u * vz;
-                sd = sqrt(rx * rx + ry * ry + rz * rz);
-            }
-        }
-        for (int o = 16; o > 0; o >>= 1) sd = fmax(sd, __shfl_xor_sync(0xffffffffu, sd, o));
-        if (lane == 0) sdev[c * (chunk / stage) + s] = (float)sd + 1.0e-3f;   // + margin (m)
-    }
+    for (int o = stage / 2; o > 0; o >>= 1) sd = fmax(sd, __shfl_xor_sync(0xffffffffu, sd, o));
+    if (j % stage == 0) sdev[c * (chunk / stage) + j / stage] = (float)sd + 1.0e-3f;  // + margin
+
+    // |e| component bounds over the chunk, rounded up by one part in 2^20 so
+    // they hold for the FP32 values
+    float mx = fabsf(e.x) * 1.000001f, my = fabsf(e.y) * 1.000001f;
+    float mz = fabsf(e.z) * 1.000001f, m2 = e.w * 1.000001f;
     for (int o = 16; o > 0; o >>= 1) {
         mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         my = fmaxf(my, __shfl_xor_sync(0xffffffffu, my, o));
         mz = fmaxf(mz, __shfl_xor_sync(0xffffffffu, mz, o));
         m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, o));
-        dev = fmax(dev, __shfl_xor_sync(0xffffffffu, dev, o));
     }
-    if (lane == 0) {
+    if (lane == 0) s_max[j / 32] = make_float4(mx, my, mz, m2);
+    __syncthreads();
+    if (j == 0) {
+        float4 m = s_max[0];
+        for (int w = 1; w < chunk / 32; ++w) {
+            m.x = fmaxf(m.x, s_max[w].x);
+            m.y = fmaxf(m.y, s_max[w].y);
+            m.z = fmaxf(m.z, s_max[w].z);
+            m.w = fmaxf(m.w, s_max[w].w);
+        }
         ChunkRef r;
-        r.emax = make_float4(mx, my, mz, m2);
+        r.emax = m;
         split_ff(x0, r.thi.x, r.tlo.x);
         split_ff(y0, r.thi.y, r.tlo.y);
         split_ff(z0, r.thi.z, r.tlo.z);
-        r.thi.w = (float)dev + 1.0e-3f;     // chord deviation + margin (m)
-        r.tlo.w = 0.f;
+        r.thi.w = r.tlo.w = 0.f;
         ctab[c] = r;
     }
 }
@@ -341,9 +329,11 @@ int launch_chunk_table(const SceneParams &P, int chunk, int stage, bool paired, 
                        const MixedLayout &L, cudaStream_t stream)
 {
     const int64_t nchunks = (P.naz + chunk - 1) / chunk;
-    const int warps = 8;
-    const int64_t blocks = (nchunks + warps - 1) / warps;
-    chunk_table_kernel<<<(unsigned)blocks, warps * 32, 0, stream>>>(
+    if (nchunks > 0x7fffffffLL) {
+        set_error("chunk table: %lld chunks exceed the launch limit", (long long)nchunks);
+        return SARBP_ERANGE;
+    }
+    chunk_table_kernel<<<(unsigned)nchunks, chunk, 0, stream>>>(
         P, chunk, stage, paired ? 1 : 0, reinterpret_cast<float4 *>(ws + L.ptab),
         reinterpret_cast<PulseFF *>(ws + L.pff), reinterpret_cast<ChunkRef *>(ws + L.ctab),
         reinterpret_cast<float *>(ws + L.sdev), nchunks);

@@ -37,6 +37,7 @@
 #include <climits>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -186,6 +187,7 @@ struct StagedShared {
     unsigned long long lane_key[kMaxTileThreads];   // lane assignment sort
     long long lo, hi;                 // tile-wide pulse range
     long long item[2];                // persistent kernels: current work item
+    float2 zero;                      // read by masked-off pulses of the fast path
 };
 
 struct StagedCta {
@@ -413,9 +415,11 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                 const bool win_ok = sh.wlo[q] >= 0 && (int64_t)sh.whi[q] <= P.nra - 2 &&
                                     sh.whi[q] - b0 < W;
                 const bool exact = work && S.exact;
-                const bool fast = __all_sync(0xffffffffu, !work || (jmin == 0 &&
-                                                                    jmax == STAGE - 1 &&
-                                                                    win_ok && !exact));
+                // fast path: the window holds every bin the warp's pixels can
+                // reach; pulses outside a lane's aperture are masked off
+                const bool fast = __all_sync(0xffffffffu, !work || (win_ok && !exact));
+                const bool whole = __all_sync(0xffffffffu,
+                                              !work || (jmin == 0 && jmax == STAGE - 1));
                 if (!__any_sync(0xffffffffu, work)) {
                     // no pixel of this warp has pulses in the stage
                 } else if (exact) {
@@ -440,56 +444,76 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                     const float tie = 0.5f - S.eps;
                     float sre = gre, sim = gim;
                     uint32_t amb_mask = 0, miss_mask = 0, valid_mask;
+                    // pulses of the stage inside this lane's aperture
+                    const uint32_t apmask =
+                        work ? (((jmax == 31) ? 0xffffffffu : ((1u << (jmax + 1)) - 1u)) &
+                                ~((1u << jmin) - 1u))
+                             : 0u;
                     if (fast) {
                         // two pulses per f32x2 instruction, the scalar path's
-                        // operation sequence per pulse (bit-identical values)
-                        valid_mask = STAGE == 32 ? 0xffffffffu : (1u << STAGE) - 1u;
+                        // operation sequence per pulse (bit-identical values);
+                        // MASKED reads the zero slot for pulses outside a
+                        // lane's aperture
+                        valid_mask = apmask;
                         const f2_t mx2 = C.mx, my2 = C.my, mz2 = C.mz;
                         const f2_t c1_2 = C.c1, c2_2 = C.c2, c3_2 = C.c3;
                         const f2_t g0_2 = C.g0, a_2 = C.a, r0sq2 = C.r0sq;
                         const f2_t idra2 = P.inv_dra_f2, beta2 = P.beta_f2, magic2 = P.magic_f2;
                         const ulonglong2 *sp = reinterpret_cast<const ulonglong2 *>(stab);
                         float rmax = 0.f;     // largest |g - rint(g)|: a tie test per stage
+                        auto pulse_pairs = [&](auto masked_tag) {
+                            constexpr bool MASKED = decltype(masked_tag)::value;
 #pragma unroll
-                        for (int p = 0; p < STAGE / 2; ++p) {
-                            const ulonglong2 exy = sp[2 * p], ezw = sp[2 * p + 1];
-                            f2_t D2 = f2_fma(mz2, ezw.x, ezw.y);
-                            D2 = f2_fma(my2, exy.y, D2);
-                            D2 = f2_fma(mx2, exy.x, D2);
-                            f2_t q2 = f2_fma(c3_2, D2, c2_2);
-                            q2 = f2_fma(q2, D2, c1_2);
-                            const f2_t dR2 = f2_mul(D2, q2);
-                            const f2_t g2 = f2_fma(dR2, idra2, g0_2);
-                            const f2_t t2 = f2_add(g2, magic2);
-                            const f2_t r2 = f2_sub(g2, f2_sub(t2, magic2));
-                            float t0, t1, r0, r1;
-                            f2_unpack(t2, t0, t1);
-                            f2_unpack(r2, r0, r1);
-                            rmax = fmaxf(rmax, fmaxf(fabsf(r0), fabsf(r1)));
-                            const int col0 =
-                                (int)min((unsigned)(__float_as_int(t0) + colbias), (unsigned)(W - 1));
-                            const int col1 =
-                                (int)min((unsigned)(__float_as_int(t1) + colbias), (unsigned)(W - 1));
-                            const float2 v0 = sraw[(2 * p) * W + col0];
-                            const float2 v1 = sraw[(2 * p + 1) * W + col1];
-                            const f2_t ph2 = f2_mul(dR2, f2_fma(beta2, dR2, a_2));
-                            float ph0, ph1, s0, c0, s1, c1;
-                            f2_unpack(ph2, ph0, ph1);
-                            __sincosf(ph0, &s0, &c0);
-                            __sincosf(ph1, &s1, &c1);
-                            const f2_t w2 = f2_add(r0sq2, D2);
-                            float wc0, wc1, ws0, ws1;
-                            f2_unpack(f2_mul(w2, f2_pack(c0, c1)), wc0, wc1);
-                            f2_unpack(f2_mul(w2, f2_pack(s0, s1)), ws0, ws1);
-                            sre = fmaf(v0.x, wc0, fmaf(v0.y, ws0, sre));
-                            sim = fmaf(v0.y, wc0, fmaf(-v0.x, ws0, sim));
-                            sre = fmaf(v1.x, wc1, fmaf(v1.y, ws1, sre));
-                            sim = fmaf(v1.y, wc1, fmaf(-v1.x, ws1, sim));
-                            if (kChecksum && work) {
-                                cs += mix64(K + 2 * p, col0 + b0);
-                                cs += mix64(K + 2 * p + 1, col1 + b0);
+                            for (int p = 0; p < STAGE / 2; ++p) {
+                                const ulonglong2 exy = sp[2 * p], ezw = sp[2 * p + 1];
+                                f2_t D2 = f2_fma(mz2, ezw.x, ezw.y);
+                                D2 = f2_fma(my2, exy.y, D2);
+                                D2 = f2_fma(mx2, exy.x, D2);
+                                f2_t q2 = f2_fma(c3_2, D2, c2_2);
+                                q2 = f2_fma(q2, D2, c1_2);
+                                const f2_t dR2 = f2_mul(D2, q2);
+                                const f2_t g2 = f2_fma(dR2, idra2, g0_2);
+                                const f2_t t2 = f2_add(g2, magic2);
+                                const f2_t r2 = f2_sub(g2, f2_sub(t2, magic2));
+                                float t0, t1, r0, r1;
+                                f2_unpack(t2, t0, t1);
+                                f2_unpack(r2, r0, r1);
+                                rmax = fmaxf(rmax, fmaxf(fabsf(r0), fabsf(r1)));
+                                const int col0 = (int)min((unsigned)(__float_as_int(t0) + colbias),
+                                                          (unsigned)(W - 1));
+                                const int col1 = (int)min((unsigned)(__float_as_int(t1) + colbias),
+                                                          (unsigned)(W - 1));
+                                const float2 *a0 = &sraw[(2 * p) * W + col0];
+                                const float2 *a1 = &sraw[(2 * p + 1) * W + col1];
+                                if (MASKED) {
+                                    if (!((apmask >> (2 * p)) & 1u)) a0 = &sh.zero;
+                                    if (!((apmask >> (2 * p + 1)) & 1u)) a1 = &sh.zero;
+                                }
+                                const float2 v0 = *a0, v1 = *a1;
+                                const f2_t ph2 = f2_mul(dR2, f2_fma(beta2, dR2, a_2));
+                                float ph0, ph1, s0, c0, s1, c1;
+                                f2_unpack(ph2, ph0, ph1);
+                                __sincosf(ph0, &s0, &c0);
+                                __sincosf(ph1, &s1, &c1);
+                                const f2_t w2 = f2_add(r0sq2, D2);
+                                float wc0, wc1, ws0, ws1;
+                                f2_unpack(f2_mul(w2, f2_pack(c0, c1)), wc0, wc1);
+                                f2_unpack(f2_mul(w2, f2_pack(s0, s1)), ws0, ws1);
+                                sre = fmaf(v0.x, wc0, fmaf(v0.y, ws0, sre));
+                                sim = fmaf(v0.y, wc0, fmaf(-v0.x, ws0, sim));
+                                sre = fmaf(v1.x, wc1, fmaf(v1.y, ws1, sre));
+                                sim = fmaf(v1.y, wc1, fmaf(-v1.x, ws1, sim));
+                                if (kChecksum) {
+                                    if ((apmask >> (2 * p)) & 1u) cs += mix64(K + 2 * p, col0 + b0);
+                                    if ((apmask >> (2 * p + 1)) & 1u)
+                                        cs += mix64(K + 2 * p + 1, col1 + b0);
+                                }
                             }
-                        }
+                        };
+                        if (whole)
+                            pulse_pairs(std::false_type{});
+                        else
+                            pulse_pairs(std::true_type{});
                         if (work && rmax > tie) {
                             // a pulse near a .5 tie (rare): find which
                             for (int j = 0; j < STAGE; ++j) {
@@ -498,15 +522,11 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                                 bool amb;
                                 pulse_eval(C, stage_e(stab, j), P.inv_dra_f, colbias, tie, D, dR,
                                            col, amb);
-                                if (amb) amb_mask |= 1u << j;
+                                if (amb && ((apmask >> j) & 1u)) amb_mask |= 1u << j;
                             }
                         }
                     } else {
                         valid_mask = 0;
-                        const uint32_t apmask =
-                            work ? (((jmax == 31) ? 0xffffffffu : ((1u << (jmax + 1)) - 1u)) &
-                                    ~((1u << jmin) - 1u))
-                                 : 0u;
 #pragma unroll
                         for (int j = 0; j < STAGE; ++j) {
                             float D, dR;
@@ -647,6 +667,7 @@ __device__ __forceinline__ StagedCta staged_cta_init(unsigned char *smem_dyn, St
             sh.issued[b] = 0;
         }
         sh.stop = 0;
+        sh.zero = make_float2(0.f, 0.f);
         mbar_fence_init();
     }
     __syncthreads();
