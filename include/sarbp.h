@@ -188,6 +188,31 @@ SARBP_API int sarbp_focus_mixed_prepared(const sarbp_scene *scene, const sarbp_t
 SARBP_API int sarbp_mixed_status(void *workspace, size_t workspace_bytes, void *stream);
 
 /*
+ * Range bins the focusing can read: a superset [range[0], range[1]] of every
+ * valid range bin of every (pixel, pulse) pair inside the pixels' apertures,
+ * from the pulse-segment bounds the staged kernels use for their windows
+ * (endpoint and closest-point distances plus the chord deviation, one bin of
+ * margin each side).  `workspace` must hold tables prepared by
+ * sarbp_mixed_prepare with a staged tuning; `scene->raw` is not read.
+ * Synchronises `stream`; range[0] > range[1] when no pixel has an aperture.
+ * With it a caller uploads only the reachable part of each pulse row
+ * (sarbp_upload_raw_bins): the kernels never read outside it.  No reference
+ * counterpart (the reference reads Raw_Data where it lies).
+ */
+SARBP_API int sarbp_raw_bin_range(const sarbp_scene *scene, const sarbp_tuning *tuning,
+                                  void *workspace, size_t workspace_bytes, int64_t *range,
+                                  void *stream);
+
+/*
+ * Host -> device copy of range bins [bin_lo, bin_lo + nbins) of `npulses`
+ * pulse rows (complex64, row pitches in elements) into the same positions of
+ * a device raw buffer: one 2-D copy, asynchronous when `src` is pinned.
+ */
+SARBP_API int sarbp_upload_raw_bins(void *dst, int64_t dst_pitch, const void *src,
+                                    int64_t src_pitch, int64_t bin_lo, int64_t nbins,
+                                    int64_t npulses, void *stream);
+
+/*
  * Batches: many scenes of uneven size in one persistent launch.
  * Replaces the reference's per-batch host loops (gpu_small_dataset.py:285-339,
  * main_gpu.py:415-586), which launch one kernel per pixel batch and copy

@@ -276,6 +276,40 @@ SARBP_API int sarbp_mixed_status(void *workspace, size_t workspace_bytes, void *
     return SARBP_ETIMEOUT;
 }
 
+SARBP_API int sarbp_raw_bin_range(const sarbp_scene *scene, const sarbp_tuning *tuning,
+                                  void *workspace, size_t workspace_bytes, int64_t *range,
+                                  void *stream)
+{
+    SceneParams P;
+    sarbp_tuning T;
+    int rc = mixed_args(scene, tuning, &P, &T);
+    if (rc) return rc;
+    return raw_bin_range(P, T, workspace, workspace_bytes, range,
+                         static_cast<cudaStream_t>(stream));
+}
+
+SARBP_API int sarbp_upload_raw_bins(void *dst, int64_t dst_pitch, const void *src,
+                                    int64_t src_pitch, int64_t bin_lo, int64_t nbins,
+                                    int64_t npulses, void *stream)
+{
+    if (!dst || !src || dst_pitch <= 0 || src_pitch <= 0 || bin_lo < 0 || nbins < 0 ||
+        npulses < 0 || bin_lo + nbins > dst_pitch || bin_lo + nbins > src_pitch) {
+        set_error("sarbp_upload_raw_bins: bad pointers or bin range [%lld, +%lld) for pitches "
+                  "%lld / %lld",
+                  (long long)bin_lo, (long long)nbins, (long long)dst_pitch,
+                  (long long)src_pitch);
+        return SARBP_EINVAL;
+    }
+    if (nbins == 0 || npulses == 0) return SARBP_OK;
+    const size_t e = 8;   // complex64
+    return cuda_status(
+        cudaMemcpy2DAsync(static_cast<char *>(dst) + (size_t)bin_lo * e, (size_t)dst_pitch * e,
+                          static_cast<const char *>(src) + (size_t)bin_lo * e,
+                          (size_t)src_pitch * e, (size_t)nbins * e, (size_t)npulses,
+                          cudaMemcpyHostToDevice, static_cast<cudaStream_t>(stream)),
+        "sarbp_upload_raw_bins");
+}
+
 SARBP_API int64_t sarbp_tile_count(const sarbp_scene *scene, const sarbp_tuning *tuning)
 {
     SceneParams P;

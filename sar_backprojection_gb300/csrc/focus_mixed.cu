@@ -340,6 +340,93 @@ int launch_chunk_table(const SceneParams &P, int chunk, int stage, bool paired, 
     return cuda_status(cudaGetLastError(), "chunk_table launch");
 }
 
+// Bounds of the range bins a pixel can reach over its aperture, per stage of
+// `stage` pulses as in the staged kernels' window prologue, reduced to one
+// [min, max] for the scene (ints in the status block's spare words).
+__global__ void raw_bin_range_kernel(const SceneParams P, const PulseFF *__restrict__ pff,
+                                     const float *__restrict__ sdev, int stage, int *range)
+{
+    const int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int blo = INT_MAX, bhi = INT_MIN;
+    int64_t lo, hi;
+    if (ii < P.npix && pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi)) {
+        const PixelFF pf = pixel_ff(P.x[ii], P.y[ii], P.z[ii]);
+        float rmin = 3.0e38f, rmax = 0.f, dmax = 0.f;
+        for (int64_t c = lo / stage; c <= hi / stage; ++c) {
+            const int64_t K = c * stage, kb = min(K + stage - 1, P.naz - 1);
+            const float4 ta = __ldg(&pff[K].hi), tb = __ldg(&pff[kb].hi);
+            const float ax = pf.xh - ta.x, ay = pf.yh - ta.y, az = pf.zh - ta.z;
+            const float sx = tb.x - ta.x, sy = tb.y - ta.y, sz = tb.z - ta.z;
+            const float ss = sx * sx + sy * sy + sz * sz;
+            const float a2 = ax * ax + ay * ay + az * az;
+            const float d = ax * sx + ay * sy + az * sz;
+            const float u = ss > 0.f ? d / ss : 0.f;
+            const float bx = ax - sx, by = ay - sy, bz = az - sz;
+            const float b2 = bx * bx + by * by + bz * bz;
+            const float rmin2 = (u > 0.f && u < 1.f) ? fmaf(-d, u, a2) : fminf(a2, b2);
+            rmin = fminf(rmin, sqrtf(fmaxf(rmin2, 0.f)));
+            rmax = fmaxf(rmax, sqrtf(fmaxf(a2, b2)));
+            dmax = fmaxf(dmax, __ldg(&sdev[c]));
+        }
+        blo = (int)floorf((rmin - dmax - P.near_hi) * P.inv_dra_f) - 1;
+        bhi = (int)ceilf((rmax + dmax - P.near_hi) * P.inv_dra_f) + 1;
+    }
+    blo = __reduce_min_sync(0xffffffffu, blo);
+    bhi = __reduce_max_sync(0xffffffffu, bhi);
+    if ((threadIdx.x & 31) == 0 && blo <= bhi) {
+        atomicMin(&range[0], blo);
+        atomicMax(&range[1], bhi);
+    }
+}
+
+__global__ void range_init_kernel(int *range)
+{
+    range[0] = INT_MAX;
+    range[1] = INT_MIN;
+}
+
+int raw_bin_range(const SceneParams &P, const sarbp_tuning &T, void *workspace, size_t ws_bytes,
+                  int64_t *range, cudaStream_t stream)
+{
+    const MixedLayout L = mixed_layout(P, T);
+    if (!workspace || ws_bytes < L.total || !range) {
+        set_error("sarbp_raw_bin_range: workspace (%zu < %zu bytes) or range missing", ws_bytes,
+                  L.total);
+        return SARBP_EWORKSPACE;
+    }
+    if (!T.staged) {
+        set_error("sarbp_raw_bin_range: needs tables prepared with a staged tuning");
+        return SARBP_EINVAL;
+    }
+    char *ws = static_cast<char *>(workspace);
+    int *dr = reinterpret_cast<StatusBlock *>(ws + L.status)->range;
+    range_init_kernel<<<1, 1, 0, stream>>>(dr);
+    const int64_t blocks = (P.npix + 255) / 256;
+    if (blocks > 0)
+        raw_bin_range_kernel<<<(unsigned)blocks, 256, 0, stream>>>(
+            P, reinterpret_cast<const PulseFF *>(ws + L.pff),
+            reinterpret_cast<const float *>(ws + L.sdev), T.stage, dr);
+    int rc = cuda_status(cudaGetLastError(), "raw_bin_range launch");
+    if (rc) return rc;
+    int h[2];
+    rc = cuda_status(cudaMemcpyAsync(h, dr, sizeof(h), cudaMemcpyDeviceToHost, stream),
+                     "raw_bin_range read");
+    if (rc) return rc;
+    rc = cuda_status(cudaStreamSynchronize(stream), "raw_bin_range synchronize");
+    if (rc) return rc;
+    // clear the spare words again (the status block is read by sarbp_mixed_status)
+    rc = cuda_status(cudaMemsetAsync(dr, 0, 2 * sizeof(int), stream), "raw_bin_range clear");
+    if (rc) return rc;
+    if (h[0] > h[1]) {
+        range[0] = 1;
+        range[1] = 0;
+        return SARBP_OK;
+    }
+    range[0] = h[0] < 0 ? 0 : h[0];
+    range[1] = (int64_t)h[1] > P.nra - 1 ? P.nra - 1 : h[1];
+    return SARBP_OK;
+}
+
 static int check_workspace(const MixedLayout &L, void *workspace, size_t ws_bytes)
 {
     if (!workspace || ws_bytes < L.total) {

@@ -99,7 +99,8 @@ __device__ inline int64_t exact_bin(double px, double py, double pz,
 struct StatusBlock {
     unsigned int error;      // non-zero: a bounded wait gave up
     unsigned int where;      // tag of the wait that gave up
-    unsigned int pad[62];
+    int range[2];            // sarbp_raw_bin_range's reduction (0 between uses)
+    unsigned int pad[60];
 };
 
 }  // namespace sarbp
@@ -132,6 +133,8 @@ MixedLayout mixed_layout(const SceneParams &P, const sarbp_tuning &T);
 
 int launch_focus_fp64(const SceneParams &P, double *out, int32_t *nvalid, uint64_t *checksum,
                       cudaStream_t stream);
+int raw_bin_range(const SceneParams &P, const sarbp_tuning &T, void *workspace, size_t ws_bytes,
+                  int64_t *range, cudaStream_t stream);
 int launch_mixed_prepare(const SceneParams &P, const sarbp_tuning &T, void *workspace,
                          size_t ws_bytes, cudaStream_t stream);
 int launch_mixed_main(const SceneParams &P, const sarbp_tuning &T, void *workspace,

@@ -117,6 +117,10 @@ def focus(scene: DeviceScene, precision: str = "fp64", *, tuning=None,
     return res
 
 
+# bytes moved and raw bins uploaded by the last FocalizzatoreBpPx call
+last_call: dict = {}
+
+
 def FocalizzatoreBpPx(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
                       near_range, dra, lambda_val, Sint, *, precision: str = "fp64",
                       tuning=None, device=None) -> np.ndarray:
@@ -125,9 +129,11 @@ def FocalizzatoreBpPx(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
     Drop-in for sar_focuser_puntual_noui.py:149 (same positional arguments).
     """
     scene = scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
-                            near_range, dra, lambda_val, Sint, device=device)
-    res = focus(scene, precision, tuning=tuning)
+                            near_range, dra, lambda_val, Sint, device=device, raw_bins="reached")
+    res = focus(scene, precision, tuning=tuning, workspace=scene.workspace)
     img = res.to_numpy(scene.dim0, scene.dim1)
+    last_call.update(h2d_bytes=scene.h2d_bytes, d2h_bytes=img.nbytes,
+                     raw_bins=(scene.bin_lo, scene.bin_hi))
     res.check()          # a device wait that gave up leaves an incomplete image
     return img
 

@@ -11,6 +11,7 @@ Nra is odd.
 """
 from __future__ import annotations
 
+import ctypes as C
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -96,6 +97,13 @@ class DeviceScene:
     delta_range: float
     lambda_: float
     _struct: _lib.Scene | None = field(default=None, repr=False)
+    # raw_bins="reached" uploads: range bins [bin_lo, bin_hi] of every pulse
+    # are on the device (the rest of each row is never read), the bytes copied
+    # host -> device, and the mixed workspace prepared on the way
+    bin_lo: int = 0
+    bin_hi: int = -1
+    h2d_bytes: int = 0
+    workspace: torch.Tensor | None = field(default=None, repr=False)
 
     @property
     def npix(self) -> int:
@@ -140,15 +148,64 @@ class DeviceScene:
         return sum(t.numel() * t.element_size() for t in ts)
 
 
+def _pulse_major_host(raw):
+    """(Naz, Nra) C-contiguous complex64 host view of an F-order (Nra, Naz)
+    raw array, or None when the host layout does not allow it."""
+    if isinstance(raw, torch.Tensor):
+        if raw.device.type != "cpu" or raw.dtype != torch.complex64:
+            return None
+        t = raw.t()
+    else:
+        a = np.asarray(raw)
+        if a.dtype != np.complex64 or not a.flags.f_contiguous:
+            return None
+        t = torch.from_numpy(a.T)
+    return t if t.is_contiguous() else None
+
+
+def _upload_reached_bins(scene: "DeviceScene", host_rows: torch.Tensor) -> None:
+    """Copy only the range bins the focusing can read (sarbp_raw_bin_range)
+    of every pulse row into the scene's (uninitialised) raw buffer."""
+    from .focuser import resolve_tuning
+    lib = _lib.load()
+    dev = scene.device
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    t = resolve_tuning(None)
+    sc = C.byref(scene.struct())
+    need = _lib.check(int(lib.sarbp_mixed_workspace_size(sc, C.byref(t))))
+    ws = torch.empty(need, dtype=torch.uint8, device=dev)
+    _lib.check(lib.sarbp_mixed_prepare(sc, C.byref(t), ws.data_ptr(), need, stream))
+    rng = (C.c_int64 * 2)()
+    _lib.check(lib.sarbp_raw_bin_range(sc, C.byref(t), ws.data_ptr(), need, rng, stream))
+    lo, hi = int(rng[0]), int(rng[1])
+    if hi >= lo:
+        _lib.check(lib.sarbp_upload_raw_bins(scene.raw.data_ptr(), scene.pitch,
+                                             host_rows.data_ptr(), scene.nra, lo, hi - lo + 1,
+                                             scene.naz, stream))
+    scene.bin_lo, scene.bin_hi = lo, hi
+    scene.h2d_bytes += max(0, hi - lo + 1) * scene.naz * 8
+    scene.workspace = ws
+
+
 def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
-                    near_range, dra, lambda_val, Sint, device=None) -> DeviceScene:
+                    near_range, dra, lambda_val, Sint, device=None,
+                    raw_bins: str = "all") -> DeviceScene:
     """Upload the reference's 13 focusing arguments (same order) to the device.
 
     Raises ValueError where the reference does (Raw_Data or xxg1 not 2-D,
     sar_focuser_puntual_noui.py:163-170) and for arrays whose sizes do not
     match the DEM grid or a trajectory shorter than Naz (where the reference
     would fail with an IndexError inside its pixel loop).
+
+    ``raw_bins="reached"``: when the raw data are a host array in the
+    reference's column-major layout, only the range bins some pixel's
+    aperture can reach are copied (a bound computed on the device from the
+    DEM, apertures and trajectory, with margins); the kernels never read the
+    rest of the device buffer.  Other layouts, and device inputs, are taken
+    whole.
     """
+    if raw_bins not in ("all", "reached"):
+        raise ValueError(f"raw_bins must be 'all' or 'reached', got {raw_bins!r}")
     raw_shape = tuple(Raw_Data.shape)
     if len(raw_shape) != 2:
         raise ValueError("Raw_Data must be a 2D array")
@@ -170,13 +227,18 @@ def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
         raise RuntimeError("sar_backprojection_gb300 needs a CUDA device (no CPU fallback)")
     device = (torch.device(device) if device is not None
               else torch.device("cuda", torch.cuda.current_device()))
-    raw_t, nra, naz, pitch = raw_to_device(Raw_Data, device)
+    host_rows = _pulse_major_host(Raw_Data) if raw_bins == "reached" else None
+    if host_rows is not None:
+        pitch = nra + (nra & 1)
+        raw_t = torch.empty((naz, pitch, 2), dtype=torch.float32, device=device)
+    else:
+        raw_t, nra, naz, pitch = raw_to_device(Raw_Data, device)
 
     def traj(w):
         t = _as_tensor(_cast_host(w, np.float64)).reshape(-1)
         return t.to(device, non_blocking=True).contiguous()
 
-    return DeviceScene(
+    scene = DeviceScene(
         dim0=dim0, dim1=dim1,
         x=flatten_f(xxg1, np.float64, device), y=flatten_f(yyg1, np.float64, device),
         z=flatten_f(zzg1, np.float64, device),
@@ -186,3 +248,15 @@ def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
         raw=raw_t, nra=nra, naz=naz, pitch=pitch,
         near_range=float(near_range), delta_range=float(dra), lambda_=float(lambda_val),
     )
+    small = sum(t.numel() * t.element_size() for t in (scene.x, scene.y, scene.z, scene.mask,
+                                                        scene.index, scene.sint, scene.tx,
+                                                        scene.ty, scene.tz))
+    if host_rows is not None:
+        scene.h2d_bytes = small
+        _upload_reached_bins(scene, host_rows)
+    else:
+        scene.bin_lo, scene.bin_hi = 0, nra - 1
+        scene.h2d_bytes = small + (nra * naz * 8 if Raw_Data is not None and
+                                   not (isinstance(Raw_Data, torch.Tensor) and
+                                        Raw_Data.device.type == "cuda") else 0)
+    return scene
