@@ -73,23 +73,24 @@ typedef struct sarbp_scene {
 /*
  * Tuning of the mixed-precision kernel.  An all-zero struct (or NULL) selects
  * the library default; sarbp_default_tuning() fills the defaults explicitly.
- * Supported: staged=0 with chunk 32/64 and tiles 32x8, 64x4, 16x16; staged=1
- * or 2 with chunk 32, 64 or 128 and (tile, window, stage) 16x16/160/32,
+ * Supported: staged=0 with chunk 32/64 and tiles 32x8, 64x4, 16x16; staged=1,
+ * 2 or 3 with chunk 32, 64 or 128 and (tile, window, stage) 16x16/160/32,
  * 16x16/160/16, 16x16/128/32, 16x8/128/32, 16x8/128/16, 32x8/128/32,
  * 64x4/128/32.  The staged kernels copy raw data in 16- or 32-pulse stages
  * through a ring of 64 pulses; the chunk is the pulse group that shares one
- * float-float reference (mid-chunk pulse).  staged=2 runs the staged kernel on a persistent grid
- * that drains a queue of the scene's tiles in decreasing estimated cost; the
- * queue (built by sarbp_mixed_prepare) adds a few bytes per tile to the
- * workspace.  Images are bit-identical across staged=1 and staged=2.
+ * float-float reference (mid-chunk pulse).  staged=2 and 3 run the staged
+ * kernel on a persistent grid that drains a queue of the scene's tiles
+ * (built by sarbp_mixed_prepare, a few bytes per tile of workspace): in
+ * decreasing estimated cost (2) or increasing last pulse (3, for streamed
+ * uploads).  Images are bit-identical across staged=1, 2 and 3.
  */
 typedef struct sarbp_tuning {
     int32_t chunk;        /* pulses per chunk: 32, 64 (128: staged only)      */
     int32_t tile0;        /* pixel-tile extent along dim0 (power of two)      */
     int32_t tile1;        /* pixel-tile extent along dim1                     */
     int32_t staged;       /* 0: L1/L2 gathers; 1: TMA-staged raw window, one CTA per
-                             tile; 2: staged, persistent grid over a cost-ordered
-                             tile queue */
+                             tile; 2 / 3: staged, persistent grid over a tile queue
+                             ordered by cost / by last pulse */
     int32_t window;       /* staged: range bins staged per pulse stage (0: default) */
     int32_t stage;        /* staged: pulses per TMA stage, 16 or 32 (0: default)   */
     int32_t wait_polls;   /* staged, diagnostic: mbarrier polls before a stage wait
@@ -186,6 +187,26 @@ SARBP_API int sarbp_focus_mixed_prepared(const sarbp_scene *scene, const sarbp_t
  * waits).
  */
 SARBP_API int sarbp_mixed_status(void *workspace, size_t workspace_bytes, void *stream);
+
+/*
+ * Streamed focusing (tuning.staged = 3: the prepared workspace holds the
+ * scene's tiles ordered by their last aperture pulse).  A caller that uploads
+ * the raw data in pulse blocks reads the queue's keys (one past each tile's
+ * last pulse, ascending; sarbp_tile_queue_keys synchronises `stream`) and
+ * launches sarbp_focus_mixed_range over the queue items whose key is covered
+ * as each block lands, so focusing overlaps the upload.  With staged = 2 the
+ * keys are the tiles' costs, descending.  No reference counterpart (the
+ * reference uploads a whole raw window before each launch,
+ * main_gpu.py:430-470).
+ */
+SARBP_API int sarbp_tile_queue_keys(const sarbp_scene *scene, const sarbp_tuning *tuning,
+                                    void *workspace, size_t workspace_bytes, uint32_t *keys,
+                                    int64_t n, void *stream);
+SARBP_API int sarbp_focus_mixed_range(const sarbp_scene *scene, const sarbp_tuning *tuning,
+                                      double *out, int32_t *nvalid, uint64_t *checksum,
+                                      uint64_t *counters, void *workspace,
+                                      size_t workspace_bytes, int64_t first, int64_t count,
+                                      void *stream);
 
 /*
  * Range bins the focusing can read: a superset [range[0], range[1]] of every

@@ -76,6 +76,10 @@ SIGNATURES = {
                                              _P, _P, C.c_size_t, _P]),
     "sarbp_probe_issue_rates": (C.c_int, [C.POINTER(C.c_double), _P]),
     "sarbp_mixed_status": (C.c_int, [_P, C.c_size_t, _P]),
+    "sarbp_tile_queue_keys": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, C.c_size_t,
+                                        C.POINTER(C.c_uint32), C.c_int64, _P]),
+    "sarbp_focus_mixed_range": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, _P, _P, _P,
+                                          _P, C.c_size_t, C.c_int64, C.c_int64, _P]),
     "sarbp_raw_bin_range": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, C.c_size_t,
                                       C.POINTER(C.c_int64), _P]),
     "sarbp_upload_raw_bins": (C.c_int, [_P, C.c_int64, _P, C.c_int64, C.c_int64, C.c_int64,

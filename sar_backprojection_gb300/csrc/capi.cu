@@ -141,8 +141,8 @@ bool valid_tuning(sarbp_tuning *t)
         set_error("tuning.stage must be 16 or 32 (got %d)", t->stage);
         return false;
     }
-    if (t->staged < 0 || t->staged > 2) {
-        set_error("tuning.staged must be 0, 1 or 2 (got %d)", t->staged);
+    if (t->staged < 0 || t->staged > 3) {
+        set_error("tuning.staged must be 0, 1, 2 or 3 (got %d)", t->staged);
         return false;
     }
     if (t->chunk != 32 && t->chunk != 64 && !(t->staged && t->chunk == 128)) {
@@ -308,6 +308,36 @@ SARBP_API int sarbp_upload_raw_bins(void *dst, int64_t dst_pitch, const void *sr
                           (size_t)src_pitch * e, (size_t)nbins * e, (size_t)npulses,
                           cudaMemcpyHostToDevice, static_cast<cudaStream_t>(stream)),
         "sarbp_upload_raw_bins");
+}
+
+SARBP_API int sarbp_focus_mixed_range(const sarbp_scene *scene, const sarbp_tuning *tuning,
+                                      double *out, int32_t *nvalid, uint64_t *checksum,
+                                      uint64_t *counters, void *workspace,
+                                      size_t workspace_bytes, int64_t first, int64_t count,
+                                      void *stream)
+{
+    SceneParams P;
+    sarbp_tuning T;
+    int rc = mixed_args(scene, tuning, &P, &T);
+    if (rc) return rc;
+    if (!out) {
+        set_error("sarbp_focus_mixed_range: out is NULL");
+        return SARBP_EINVAL;
+    }
+    return launch_mixed_range(P, T, workspace, workspace_bytes, first, count, out, nvalid,
+                              checksum, counters, static_cast<cudaStream_t>(stream));
+}
+
+SARBP_API int sarbp_tile_queue_keys(const sarbp_scene *scene, const sarbp_tuning *tuning,
+                                    void *workspace, size_t workspace_bytes, uint32_t *keys,
+                                    int64_t n, void *stream)
+{
+    SceneParams P;
+    sarbp_tuning T;
+    int rc = mixed_args(scene, tuning, &P, &T);
+    if (rc) return rc;
+    return tile_queue_keys(P, T, workspace, workspace_bytes, keys, n,
+                           static_cast<cudaStream_t>(stream));
 }
 
 SARBP_API int64_t sarbp_tile_count(const sarbp_scene *scene, const sarbp_tuning *tuning)

@@ -32,7 +32,7 @@ MixedLayout mixed_layout(const SceneParams &P, const sarbp_tuning &T)
     L.sdev = off;
     off = align256(off + sizeof(float) * (size_t)(nchunks * chunk / (T.stage > 0 ? T.stage : 32)));
     L.base = off;
-    if (T.staged == 2 && T.tile0 > 0 && T.tile1 > 0) {
+    if (T.staged >= 2 && T.tile0 > 0 && T.tile1 > 0) {
         const int64_t nt = ((P.dim0 + T.tile0 - 1) / T.tile0) * ((P.dim1 + T.tile1 - 1) / T.tile1);
         L.ntiles = nt;
         L.keys_in = off;
@@ -322,8 +322,8 @@ static int launch_gather(const SceneParams &P, const MixedLayout &L, char *ws, d
 }
 
 int launch_staged(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L, char *ws,
-                  bool queued, double *out, int32_t *nvalid, uint64_t *checksum,
-                  uint64_t *counters, cudaStream_t stream);
+                  bool queued, int64_t first, int64_t count, double *out, int32_t *nvalid,
+                  uint64_t *checksum, uint64_t *counters, cudaStream_t stream);
 
 int launch_chunk_table(const SceneParams &P, int chunk, int stage, bool paired, char *ws,
                        const MixedLayout &L, cudaStream_t stream)
@@ -452,7 +452,7 @@ int launch_mixed_prepare(const SceneParams &P, const sarbp_tuning &T, void *work
     rc = launch_chunk_table(P, T.chunk, T.stage > 0 ? T.stage : 32, T.staged != 0, ws, L, stream);
     if (rc) return rc;
     // persistent staged path: tiles in decreasing estimated cost
-    if (T.staged == 2) return tile_order(P, T, L, ws, stream);
+    if (T.staged >= 2) return tile_order(P, T, L, ws, stream);
     return SARBP_OK;
 }
 
@@ -473,7 +473,8 @@ int launch_mixed_main(const SceneParams &P, const sarbp_tuning &T, void *workspa
         SceneParams Ps = P;
         Ps.wait_polls = T.wait_polls > 0 ? (uint32_t)T.wait_polls : (1u << 22);
         Ps.withhold = T.withhold;
-        return launch_staged(Ps, T, L, ws, T.staged == 2, out, nvalid, checksum, counters, stream);
+        return launch_staged(Ps, T, L, ws, T.staged >= 2, 0, L.ntiles, out, nvalid, checksum,
+                             counters, stream);
     }
     const int key = T.chunk * 1000000 + T.tile0 * 1000 + T.tile1;
     switch (key) {
@@ -494,6 +495,50 @@ int launch_mixed_main(const SceneParams &P, const sarbp_tuning &T, void *workspa
                       T.tile0, T.tile1);
             return SARBP_EINVAL;
     }
+}
+
+}  // namespace sarbp
+
+namespace sarbp {
+
+// Queue items [first, first + count) of a workspace prepared with staged >= 2.
+int launch_mixed_range(const SceneParams &P, const sarbp_tuning &T, void *workspace,
+                       size_t ws_bytes, int64_t first, int64_t count, double *out,
+                       int32_t *nvalid, uint64_t *checksum, uint64_t *counters,
+                       cudaStream_t stream)
+{
+    if (T.staged < 2) {
+        set_error("sarbp_focus_mixed_range: needs a queued tuning (staged 2 or 3)");
+        return SARBP_EINVAL;
+    }
+    const MixedLayout L = mixed_layout(P, T);
+    int rc = check_workspace(L, workspace, ws_bytes);
+    if (rc) return rc;
+    SceneParams Ps = P;
+    Ps.wait_polls = T.wait_polls > 0 ? (uint32_t)T.wait_polls : (1u << 22);
+    Ps.withhold = T.withhold;
+    return launch_staged(Ps, T, L, static_cast<char *>(workspace), true, first, count, out,
+                         nvalid, checksum, counters, stream);
+}
+
+// The prepared queue's sorted keys (staged=2: tile costs, staged=3: one past
+// each tile's last pulse) into host memory; synchronises the stream.
+int tile_queue_keys(const SceneParams &P, const sarbp_tuning &T, void *workspace,
+                    size_t ws_bytes, uint32_t *keys, int64_t n, cudaStream_t stream)
+{
+    const MixedLayout L = mixed_layout(P, T);
+    int rc = check_workspace(L, workspace, ws_bytes);
+    if (rc) return rc;
+    if (T.staged < 2 || !keys || n != L.ntiles) {
+        set_error("sarbp_tile_queue_keys: needs a queued tuning and %lld keys",
+                  (long long)L.ntiles);
+        return SARBP_EINVAL;
+    }
+    rc = cuda_status(cudaMemcpyAsync(keys, static_cast<char *>(workspace) + L.keys_out,
+                                     sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToHost, stream),
+                     "tile queue keys read");
+    if (rc) return rc;
+    return cuda_status(cudaStreamSynchronize(stream), "tile queue keys synchronize");
 }
 
 }  // namespace sarbp

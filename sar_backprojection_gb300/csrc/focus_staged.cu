@@ -64,19 +64,19 @@ SARBP_STAGED_CHUNK_EXTERN(extern, 64)
 SARBP_STAGED_CHUNK_EXTERN(extern, 128)
 
 int launch_staged(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L, char *ws,
-                  bool queued, double *out, int32_t *nvalid, uint64_t *checksum,
-                  uint64_t *counters, cudaStream_t stream)
+                  bool queued, int64_t first, int64_t count, double *out, int32_t *nvalid,
+                  uint64_t *checksum, uint64_t *counters, cudaStream_t stream)
 {
     switch (T.chunk) {
         case 32:
-            return launch_staged_chunk<32>(P, T, L, ws, queued, out, nvalid, checksum, counters,
-                                           stream);
+            return launch_staged_chunk<32>(P, T, L, ws, queued, first, count, out, nvalid,
+                                           checksum, counters, stream);
         case 64:
-            return launch_staged_chunk<64>(P, T, L, ws, queued, out, nvalid, checksum, counters,
-                                           stream);
+            return launch_staged_chunk<64>(P, T, L, ws, queued, first, count, out, nvalid,
+                                           checksum, counters, stream);
         case 128:
-            return launch_staged_chunk<128>(P, T, L, ws, queued, out, nvalid, checksum, counters,
-                                            stream);
+            return launch_staged_chunk<128>(P, T, L, ws, queued, first, count, out, nvalid,
+                                            checksum, counters, stream);
         default:
             set_error("staged path: unsupported chunk %d", T.chunk);
             return SARBP_EINVAL;
@@ -212,7 +212,10 @@ int tile_costs(const SceneParams &P, const sarbp_tuning &T, int64_t *costs, cuda
     return SARBP_EINVAL;
 }
 
-template <int T0, int T1>
+// Queue key of each tile: its estimated cost (sum of its pixels' kept
+// aperture lengths) or, with kEnd, one past its last kept pulse (0 for a tile
+// without apertures).
+template <int T0, int T1, bool kEnd>
 __global__ void tile_key_kernel(const SceneParams P, int64_t ntile0, int64_t ntiles,
                                 uint32_t *__restrict__ keys, int32_t *__restrict__ ids)
 {
@@ -226,8 +229,12 @@ __global__ void tile_key_kernel(const SceneParams P, int64_t ntile0, int64_t nti
             if (i0 >= P.dim0 || i1 >= P.dim1) continue;
             const int64_t ii = i0 + P.dim0 * i1;
             int64_t lo, hi;
-            if (pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi))
-                c += (uint64_t)(hi - lo + 1);
+            if (pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi)) {
+                if (kEnd)
+                    c = c > (uint64_t)(hi + 1) ? c : (uint64_t)(hi + 1);
+                else
+                    c += (uint64_t)(hi - lo + 1);
+            }
         }
     keys[tile] = c > 0xffffffffull ? 0xffffffffu : (uint32_t)c;
     ids[tile] = (int32_t)tile;
@@ -235,15 +242,20 @@ __global__ void tile_key_kernel(const SceneParams P, int64_t ntile0, int64_t nti
 
 size_t tile_sort_bytes(int64_t ntiles)
 {
-    size_t b = 0;
-    cub::DeviceRadixSort::SortPairsDescending((void *)nullptr, b, (const uint32_t *)nullptr,
+    size_t a = 0, b = 0;
+    cub::DeviceRadixSort::SortPairsDescending((void *)nullptr, a, (const uint32_t *)nullptr,
                                               (uint32_t *)nullptr, (const int32_t *)nullptr,
                                               (int32_t *)nullptr, (int)ntiles);
-    return b;
+    cub::DeviceRadixSort::SortPairs((void *)nullptr, b, (const uint32_t *)nullptr,
+                                    (uint32_t *)nullptr, (const int32_t *)nullptr,
+                                    (int32_t *)nullptr, (int)ntiles);
+    return a > b ? a : b;
 }
 
-// Tiles in decreasing estimated cost (their pixels' kept aperture lengths)
-// into the workspace queue: key kernel + device radix sort, stream-ordered.
+// The workspace tile queue: staged=2 in decreasing estimated cost (longest
+// tiles first), staged=3 in increasing last pulse (a tile can run as soon as
+// the raw rows up to its last pulse are resident); key kernel + device radix
+// sort, stream-ordered.
 int tile_order(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L, char *ws,
                cudaStream_t stream)
 {
@@ -257,10 +269,16 @@ int tile_order(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L
     auto *keys_in = reinterpret_cast<uint32_t *>(ws + L.keys_in);
     auto *vals_in = reinterpret_cast<int32_t *>(ws + L.vals_in);
     const unsigned blocks = (unsigned)((nt + 127) / 128);
+    const bool by_end = T.staged == 3;
     bool launched = false;
 #define X(A, B)                                                                             \
     if (!launched && T.tile0 == A && T.tile1 == B) {                                        \
-        tile_key_kernel<A, B><<<blocks, 128, 0, stream>>>(P, nt0, nt, keys_in, vals_in);    \
+        if (by_end)                                                                         \
+            tile_key_kernel<A, B, true><<<blocks, 128, 0, stream>>>(P, nt0, nt, keys_in,    \
+                                                                    vals_in);               \
+        else                                                                                \
+            tile_key_kernel<A, B, false><<<blocks, 128, 0, stream>>>(P, nt0, nt, keys_in,   \
+                                                                     vals_in);              \
         launched = true;                                                                    \
     }
     X(16, 16) X(16, 8) X(32, 8) X(64, 4)
@@ -272,11 +290,15 @@ int tile_order(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L
     int rc = cuda_status(cudaGetLastError(), "tile_key launch");
     if (rc) return rc;
     size_t tmp = L.sort_tmp_bytes;
-    return cuda_status(cub::DeviceRadixSort::SortPairsDescending(
-                           ws + L.sort_tmp, tmp, keys_in,
-                           reinterpret_cast<uint32_t *>(ws + L.keys_out), vals_in,
-                           reinterpret_cast<int32_t *>(ws + L.vals_out), (int)nt, 0, 32, stream),
-                       "tile order sort");
+    auto *keys_out = reinterpret_cast<uint32_t *>(ws + L.keys_out);
+    auto *vals_out = reinterpret_cast<int32_t *>(ws + L.vals_out);
+    const cudaError_t e =
+        by_end ? cub::DeviceRadixSort::SortPairs(ws + L.sort_tmp, tmp, keys_in, keys_out, vals_in,
+                                                 vals_out, (int)nt, 0, 32, stream)
+               : cub::DeviceRadixSort::SortPairsDescending(ws + L.sort_tmp, tmp, keys_in,
+                                                           keys_out, vals_in, vals_out, (int)nt,
+                                                           0, 32, stream);
+    return cuda_status(e, "tile order sort");
 }
 
 int tile_count(const SceneParams &P, const sarbp_tuning &T, int64_t *nt)

@@ -83,7 +83,7 @@ extern "C" SARBP_API int sarbp_focus_mixed_noalloc(const sarbp_scene *scene,
         return SARBP_ERANGE;
     }
     MixedLayout L = mixed_layout(P, T);
-    if (T.staged == 2 && L.total > kNoAllocBytes) {
+    if (T.staged >= 2 && L.total > kNoAllocBytes) {
         T.staged = 1;   // no room for the tile queue: one CTA per tile
         L = mixed_layout(P, T);
     }

@@ -135,6 +135,12 @@ int launch_focus_fp64(const SceneParams &P, double *out, int32_t *nvalid, uint64
                       cudaStream_t stream);
 int raw_bin_range(const SceneParams &P, const sarbp_tuning &T, void *workspace, size_t ws_bytes,
                   int64_t *range, cudaStream_t stream);
+int launch_mixed_range(const SceneParams &P, const sarbp_tuning &T, void *workspace,
+                       size_t ws_bytes, int64_t first, int64_t count, double *out,
+                       int32_t *nvalid, uint64_t *checksum, uint64_t *counters,
+                       cudaStream_t stream);
+int tile_queue_keys(const SceneParams &P, const sarbp_tuning &T, void *workspace,
+                    size_t ws_bytes, uint32_t *keys, int64_t n, cudaStream_t stream);
 int launch_mixed_prepare(const SceneParams &P, const sarbp_tuning &T, void *workspace,
                          size_t ws_bytes, cudaStream_t stream);
 int launch_mixed_main(const SceneParams &P, const sarbp_tuning &T, void *workspace,

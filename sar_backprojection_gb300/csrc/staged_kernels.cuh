@@ -744,8 +744,8 @@ template <class Cfg, bool kChecksum>
 __global__ void __launch_bounds__(Cfg::THREADS, (staged_min_blocks_single<Cfg>()))
 focus_mixed_staged_queue_kernel(const SceneParams P, const __grid_constant__ CUtensorMap raw_map,
                                 const TileTables tb, int64_t ntile0,
-                                const int32_t *__restrict__ order, int64_t ntiles,
-                                unsigned long long *cursor, const TileOutputs o,
+                                const int32_t *__restrict__ order, int64_t nitems,
+                                int64_t ntiles, unsigned long long *cursor, const TileOutputs o,
                                 unsigned long long *__restrict__ counters, StatusBlock *status)
 {
     extern __shared__ unsigned char smem_dyn[];
@@ -756,7 +756,7 @@ focus_mixed_staged_queue_kernel(const SceneParams P, const __grid_constant__ CUt
         if (threadIdx.x == 0) sh.item[round & 1] = (long long)atomicAdd(cursor, 1ull);
         __syncthreads();
         const long long item = sh.item[round & 1];
-        if (item >= ntiles) break;
+        if (item >= nitems) break;
         const int64_t tile = order[item];
         if (tile < 0 || tile >= ntiles) continue;   // a queue prepared for other pixels
         const bool ok = staged_tile<Cfg, kChecksum>(cta, P, &raw_map, tb, tile % ntile0,
@@ -873,8 +873,8 @@ inline TileTables tables_of(char *ws, const MixedLayout &L)
 
 template <class Cfg>
 int launch_staged_t(const SceneParams &P, const MixedLayout &L, char *ws, bool queued,
-                    double *out, int32_t *nvalid, uint64_t *checksum, uint64_t *counters,
-                    cudaStream_t stream)
+                    int64_t first, int64_t count, double *out, int32_t *nvalid,
+                    uint64_t *checksum, uint64_t *counters, cudaStream_t stream)
 {
     constexpr int T0 = Cfg::T0, T1 = Cfg::T1;
     const int64_t nt0 = (P.dim0 + T0 - 1) / T0, nt1 = (P.dim1 + T1 - 1) / T1;
@@ -908,13 +908,19 @@ int launch_staged_t(const SceneParams &P, const MixedLayout &L, char *ws, bool q
                                                                    Cfg::smem_bytes),
                      "queue occupancy");
     if (rc) return rc;
-    const int64_t grid = std::min<int64_t>(tiles, (int64_t)std::max(1, per_sm) * sms);
+    if (first < 0 || count < 0 || first + count > tiles || L.ntiles != tiles) {
+        set_error("staged queue: items [%lld, +%lld) outside the %lld-tile queue",
+                  (long long)first, (long long)count, (long long)tiles);
+        return SARBP_EINVAL;
+    }
+    if (count == 0) return SARBP_OK;
+    const int64_t grid = std::min<int64_t>(count, (int64_t)std::max(1, per_sm) * sms);
     auto *cursor = reinterpret_cast<unsigned long long *>(ws + L.cursor);
     rc = cuda_status(cudaMemsetAsync(cursor, 0, sizeof(*cursor), stream), "queue cursor reset");
     if (rc) return rc;
     k<<<(unsigned)grid, Cfg::THREADS, Cfg::smem_bytes, stream>>>(
-        P, map, tb, nt0, reinterpret_cast<const int32_t *>(ws + L.vals_out), tiles, cursor, o,
-        ctr, status);
+        P, map, tb, nt0, reinterpret_cast<const int32_t *>(ws + L.vals_out) + first, count,
+        tiles, cursor, o, ctr, status);
     return cuda_status(cudaGetLastError(), "focus_mixed_staged_queue launch");
 }
 
@@ -953,13 +959,15 @@ int launch_batch_t(char *bws, const BatchLayout &BL, int64_t n_items, bool diag,
 
 template <int C>
 int launch_staged_chunk(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L,
-                        char *ws, bool queued, double *out, int32_t *nvalid, uint64_t *checksum,
-                        uint64_t *counters, cudaStream_t stream)
+                        char *ws, bool queued, int64_t first, int64_t count, double *out,
+                        int32_t *nvalid, uint64_t *checksum, uint64_t *counters,
+                        cudaStream_t stream)
 {
 #define X(C_, A, B, W, S)                                                                   \
     if (T.tile0 == A && T.tile1 == B && T.window == W && T.stage == S)                      \
-        return launch_staged_t<StagedCfg<C_, A, B, W, S>>(P, L, ws, queued, out, nvalid,    \
-                                                          checksum, counters, stream);
+        return launch_staged_t<StagedCfg<C_, A, B, W, S>>(P, L, ws, queued, first, count,   \
+                                                          out, nvalid, checksum, counters,  \
+                                                          stream);
     SARBP_STAGED_TILES(X, C)
 #undef X
     set_error("staged path: unsupported tuning chunk=%d tile=%dx%d window=%d stage=%d", T.chunk,
@@ -984,8 +992,9 @@ int launch_batch_chunk(char *bws, const BatchLayout &BL, const sarbp_tuning &T, 
 
 #define SARBP_STAGED_CHUNK_EXTERN(EXT, C)                                                   \
     EXT template int launch_staged_chunk<C>(const SceneParams &, const sarbp_tuning &,      \
-                                            const MixedLayout &, char *, bool, double *,    \
-                                            int32_t *, uint64_t *, uint64_t *, cudaStream_t); \
+                                            const MixedLayout &, char *, bool, int64_t,     \
+                                            int64_t, double *, int32_t *, uint64_t *,       \
+                                            uint64_t *, cudaStream_t);                      \
     EXT template int launch_batch_chunk<C>(char *, const BatchLayout &, const sarbp_tuning &, \
                                            int64_t, bool, uint64_t *, cudaStream_t);
 

@@ -22,7 +22,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .scene import DeviceScene, scene_to_device
+from .scene import DeviceScene, _pulse_major_host, scene_to_device
 
 PRECISIONS = ("fp64", "mixed")
 
@@ -127,15 +127,88 @@ def FocalizzatoreBpPx(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
     """Focus one scene; returns complex128 of xxg1's shape (column-major pixels).
 
     Drop-in for sar_focuser_puntual_noui.py:149 (same positional arguments).
+    Host raw data in the reference's column-major layout are uploaded only
+    over the range bins the apertures can reach; with ``precision="mixed"``
+    and a staged tuning the upload is streamed in pulse blocks and focusing
+    overlaps it (tiles run as soon as the pulses up to their last one are
+    resident).  The image is the same either way.
     """
+    t = resolve_tuning(tuning)
+    if precision == "mixed" and t.staged and _pulse_major_host(Raw_Data) is not None:
+        img, scene = _focus_streamed((xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz,
+                                      Raw_Data, near_range, dra, lambda_val, Sint), t, device)
+        last_call.update(h2d_bytes=scene.h2d_bytes, d2h_bytes=img.nbytes,
+                         raw_bins=(scene.bin_lo, scene.bin_hi), streamed=True)
+        return img
     scene = scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
                             near_range, dra, lambda_val, Sint, device=device, raw_bins="reached")
-    res = focus(scene, precision, tuning=tuning, workspace=scene.workspace)
+    res = focus(scene, precision, tuning=t, workspace=scene.workspace)
     img = res.to_numpy(scene.dim0, scene.dim1)
     last_call.update(h2d_bytes=scene.h2d_bytes, d2h_bytes=img.nbytes,
-                     raw_bins=(scene.bin_lo, scene.bin_hi))
+                     raw_bins=(scene.bin_lo, scene.bin_hi), streamed=False)
     res.check()          # a device wait that gave up leaves an incomplete image
     return img
+
+
+STREAM_BLOCKS = 8      # pulse blocks of a streamed drop-in upload
+
+
+def _focus_streamed(args, t: _lib.Tuning, device, blocks: int = STREAM_BLOCKS):
+    """Drop-in focusing with the raw upload overlapped by focusing.
+
+    The queue of the scene's tiles is ordered by last aperture pulse
+    (staged=3); the reachable range bins of the pulse rows go up in
+    ``blocks`` pulse blocks on a copy stream, and after each block the
+    queue items whose pulses are all resident are focused on the compute
+    stream.  Returns (image, scene).
+    """
+    lib = _lib.load()
+    tq = _lib.Tuning.from_buffer_copy(t)
+    tq.staged = 3
+    scene = scene_to_device(*args, device=device, raw_bins="bound", tuning=tq)
+    dev = scene.device
+    compute = torch.cuda.current_stream(dev)
+    sc = C.byref(scene.struct())
+    ws = scene.workspace
+    nt = _lib.check(int(lib.sarbp_tile_count(sc, C.byref(tq))))
+    keys = np.empty(nt, dtype=np.uint32)
+    _lib.check(lib.sarbp_tile_queue_keys(sc, C.byref(tq), ws.data_ptr(), ws.numel(),
+                                         keys.ctypes.data_as(C.POINTER(C.c_uint32)), nt,
+                                         compute.cuda_stream))
+    out = torch.empty((scene.npix, 2), dtype=torch.float64, device=dev)
+    lo, hi = scene.bin_lo, scene.bin_hi
+    naz = scene.naz
+    marks = [naz * (k + 1) // blocks for k in range(blocks)]
+    ends = np.searchsorted(keys, np.asarray(marks, dtype=np.int64), side="right")
+    ends[-1] = nt
+    copy = torch.cuda.Stream(dev)
+    copy.wait_stream(compute)               # raw buffer and tables allocated on compute
+    scene.raw.record_stream(copy)
+    row = scene.pitch * 8
+    first = 0
+    a0 = 0
+    for k in range(blocks):
+        a1 = marks[k]
+        if hi >= lo and a1 > a0:
+            _lib.check(lib.sarbp_upload_raw_bins(
+                scene.raw.data_ptr() + a0 * row, scene.pitch,
+                scene.host_rows.data_ptr() + a0 * scene.nra * 8, scene.nra, lo, hi - lo + 1,
+                a1 - a0, copy.cuda_stream))
+            scene.h2d_bytes += (hi - lo + 1) * (a1 - a0) * 8
+        ev = torch.cuda.Event()
+        ev.record(copy)
+        compute.wait_event(ev)
+        count = int(ends[k]) - first
+        if count > 0:
+            _lib.check(lib.sarbp_focus_mixed_range(sc, C.byref(tq), out.data_ptr(), None, None,
+                                                   None, ws.data_ptr(), ws.numel(), first,
+                                                   count, compute.cuda_stream))
+        first = int(ends[k])
+        a0 = a1
+    res = FocusResult(image=out, workspace=ws)
+    img = res.to_numpy(scene.dim0, scene.dim1)
+    res.check()
+    return img, scene
 
 
 def FocalizzatoreBpCuPy(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,

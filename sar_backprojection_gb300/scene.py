@@ -104,6 +104,7 @@ class DeviceScene:
     bin_hi: int = -1
     h2d_bytes: int = 0
     workspace: torch.Tensor | None = field(default=None, repr=False)
+    host_rows: torch.Tensor | None = field(default=None, repr=False)
 
     @property
     def npix(self) -> int:
@@ -163,14 +164,16 @@ def _pulse_major_host(raw):
     return t if t.is_contiguous() else None
 
 
-def _upload_reached_bins(scene: "DeviceScene", host_rows: torch.Tensor) -> None:
+def _upload_reached_bins(scene: "DeviceScene", host_rows: torch.Tensor, upload: bool = True,
+                         tuning=None) -> None:
     """Copy only the range bins the focusing can read (sarbp_raw_bin_range)
-    of every pulse row into the scene's (uninitialised) raw buffer."""
+    of every pulse row into the scene's (uninitialised) raw buffer; with
+    ``upload=False`` only the bound is computed (the caller copies)."""
     from .focuser import resolve_tuning
     lib = _lib.load()
     dev = scene.device
     stream = torch.cuda.current_stream(dev).cuda_stream
-    t = resolve_tuning(None)
+    t = resolve_tuning(tuning)
     sc = C.byref(scene.struct())
     need = _lib.check(int(lib.sarbp_mixed_workspace_size(sc, C.byref(t))))
     ws = torch.empty(need, dtype=torch.uint8, device=dev)
@@ -178,18 +181,19 @@ def _upload_reached_bins(scene: "DeviceScene", host_rows: torch.Tensor) -> None:
     rng = (C.c_int64 * 2)()
     _lib.check(lib.sarbp_raw_bin_range(sc, C.byref(t), ws.data_ptr(), need, rng, stream))
     lo, hi = int(rng[0]), int(rng[1])
-    if hi >= lo:
+    if upload and hi >= lo:
         _lib.check(lib.sarbp_upload_raw_bins(scene.raw.data_ptr(), scene.pitch,
                                              host_rows.data_ptr(), scene.nra, lo, hi - lo + 1,
                                              scene.naz, stream))
     scene.bin_lo, scene.bin_hi = lo, hi
-    scene.h2d_bytes += max(0, hi - lo + 1) * scene.naz * 8
+    if upload:
+        scene.h2d_bytes += max(0, hi - lo + 1) * scene.naz * 8
     scene.workspace = ws
 
 
 def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
                     near_range, dra, lambda_val, Sint, device=None,
-                    raw_bins: str = "all") -> DeviceScene:
+                    raw_bins: str = "all", tuning=None) -> DeviceScene:
     """Upload the reference's 13 focusing arguments (same order) to the device.
 
     Raises ValueError where the reference does (Raw_Data or xxg1 not 2-D,
@@ -202,10 +206,12 @@ def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
     aperture can reach are copied (a bound computed on the device from the
     DEM, apertures and trajectory, with margins); the kernels never read the
     rest of the device buffer.  Other layouts, and device inputs, are taken
-    whole.
+    whole.  ``raw_bins="bound"``: the same bound, but no raw row is copied
+    (the caller streams them; ``scene.host_rows`` is the host source) and
+    ``scene.workspace`` holds tables prepared with ``tuning``.
     """
-    if raw_bins not in ("all", "reached"):
-        raise ValueError(f"raw_bins must be 'all' or 'reached', got {raw_bins!r}")
+    if raw_bins not in ("all", "reached", "bound"):
+        raise ValueError(f"raw_bins must be 'all', 'reached' or 'bound', got {raw_bins!r}")
     raw_shape = tuple(Raw_Data.shape)
     if len(raw_shape) != 2:
         raise ValueError("Raw_Data must be a 2D array")
@@ -227,7 +233,7 @@ def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
         raise RuntimeError("sar_backprojection_gb300 needs a CUDA device (no CPU fallback)")
     device = (torch.device(device) if device is not None
               else torch.device("cuda", torch.cuda.current_device()))
-    host_rows = _pulse_major_host(Raw_Data) if raw_bins == "reached" else None
+    host_rows = _pulse_major_host(Raw_Data) if raw_bins != "all" else None
     if host_rows is not None:
         pitch = nra + (nra & 1)
         raw_t = torch.empty((naz, pitch, 2), dtype=torch.float32, device=device)
@@ -253,7 +259,8 @@ def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
                                                         scene.ty, scene.tz))
     if host_rows is not None:
         scene.h2d_bytes = small
-        _upload_reached_bins(scene, host_rows)
+        _upload_reached_bins(scene, host_rows, upload=raw_bins == "reached", tuning=tuning)
+        scene.host_rows = host_rows if raw_bins == "bound" else None
     else:
         scene.bin_lo, scene.bin_hi = 0, nra - 1
         scene.h2d_bytes = small + (nra * naz * 8 if Raw_Data is not None and

@@ -96,7 +96,9 @@ def test_workspace_size_is_host_only():
     assert n >= 16 * 40001
     t.staged = 2                               # + the tile queue: 4 arrays of 4000 tiles
     assert lib.sarbp_mixed_workspace_size(C.byref(s), C.byref(t)) >= n + 16 * 4000
-    t.staged = 3
+    t.staged = 3                               # queue ordered by last pulse: same size
+    assert lib.sarbp_mixed_workspace_size(C.byref(s), C.byref(t)) >= n + 16 * 4000
+    t.staged = 4
     assert lib.sarbp_mixed_workspace_size(C.byref(s), C.byref(t)) == _lib.SARBP_EINVAL
     assert "staged" in _lib.last_error()
     t.staged = 1

@@ -80,3 +80,20 @@ def test_drop_in_call_reports_bytes_moved():
     nra, naz = args[8].shape
     assert focuser.last_call["h2d_bytes"] < nra * naz * 8
     assert 0 <= lo <= hi < nra and img.shape == args[0].shape
+
+
+@pytest.mark.parametrize("name", sorted(SCENES))
+def test_streamed_drop_in_equals_resident_focus(name):
+    """The streamed drop-in call (pulse-block uploads overlapped by queue
+    segments) gives the resident scene's image bit for bit."""
+    args = _host_args(SCENES[name]())
+    full = scene_to_device(*args, device="cuda")
+    ref = focus(full, "mixed").check().to_numpy(full.dim0, full.dim1)
+    img = FocalizzatoreBpPx(*args, precision="mixed")
+    assert focuser.last_call["streamed"]
+    assert np.array_equal(img.view(np.uint64), ref.view(np.uint64))
+    img1 = FocalizzatoreBpPx(*args, precision="mixed",
+                             tuning=dict(chunk=128, tile0=16, tile1=8, staged=1, window=128))
+    ref1 = focus(full, "mixed", tuning=dict(chunk=128, tile0=16, tile1=8, staged=1,
+                                            window=128)).check().to_numpy(full.dim0, full.dim1)
+    assert np.array_equal(img1.view(np.uint64), ref1.view(np.uint64))
