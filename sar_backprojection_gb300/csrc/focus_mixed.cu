@@ -473,7 +473,7 @@ int launch_mixed_main(const SceneParams &P, const sarbp_tuning &T, void *workspa
         SceneParams Ps = P;
         Ps.wait_polls = T.wait_polls > 0 ? (uint32_t)T.wait_polls : (1u << 22);
         Ps.withhold = T.withhold;
-        return launch_staged(Ps, T, L, ws, T.staged >= 2, 0, L.ntiles, out, nvalid, checksum,
+        return launch_staged(Ps, T, L, ws, T.staged >= 2, 0, -1, out, nvalid, checksum,
                              counters, stream);
     }
     const int key = T.chunk * 1000000 + T.tile0 * 1000 + T.tile1;

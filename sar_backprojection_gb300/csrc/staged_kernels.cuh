@@ -717,19 +717,23 @@ constexpr int staged_min_blocks_single()
     return 512 / Cfg::THREADS > 2 ? 512 / Cfg::THREADS : 2;
 }
 
-// One scene: one CTA per pixel tile.
+// One scene: one CTA per pixel tile, tile blockIdx.x or, with a tile list,
+// list[blockIdx.x] (a segment of the prepared queue).
 template <class Cfg, bool kChecksum>
 __global__ void __launch_bounds__(Cfg::THREADS, (staged_min_blocks_single<Cfg>()))
 focus_mixed_staged_kernel(const SceneParams P, const __grid_constant__ CUtensorMap raw_map,
-                          const TileTables tb, int64_t ntile0, const TileOutputs o,
+                          const TileTables tb, int64_t ntile0, const int32_t *__restrict__ list,
+                          int64_t ntiles, const TileOutputs o,
                           unsigned long long *__restrict__ counters, StatusBlock *status)
 {
     extern __shared__ unsigned char smem_dyn[];
     __shared__ StagedShared sh;
+    const int64_t tile = list ? (int64_t)list[blockIdx.x] : (int64_t)blockIdx.x;
+    if (tile < 0 || tile >= ntiles) return;   // a list prepared for other pixels
     StagedCta cta = staged_cta_init<Cfg>(smem_dyn, sh);
     TileStats st{0, 0, 0};
-    const bool ok = staged_tile<Cfg, kChecksum>(cta, P, &raw_map, tb, blockIdx.x % ntile0,
-                                                blockIdx.x / ntile0, o, st);
+    const bool ok = staged_tile<Cfg, kChecksum>(cta, P, &raw_map, tb, tile % ntile0,
+                                                tile / ntile0, o, st);
     if (!ok) {
         staged_abort<Cfg>(cta, status, counters);
         return;
@@ -892,11 +896,21 @@ int launch_staged_t(const SceneParams &P, const MixedLayout &L, char *ws, bool q
     const TileOutputs o{reinterpret_cast<double2 *>(out), nvalid, checksum};
     auto *status = reinterpret_cast<StatusBlock *>(ws + L.status);
     auto *ctr = reinterpret_cast<unsigned long long *>(counters);
-    if (!queued) {
+    if (count < 0) count = tiles - first;   // the rest of the scene
+    if (first < 0 || count < 0 || first + count > tiles || (queued && L.ntiles != tiles)) {
+        set_error("staged launch: items [%lld, +%lld) outside the %lld-tile scene",
+                  (long long)first, (long long)count, (long long)tiles);
+        return SARBP_EINVAL;
+    }
+    if (count == 0) return SARBP_OK;
+    const int32_t *order = reinterpret_cast<const int32_t *>(ws + L.vals_out);
+    if (!queued || count < tiles) {
+        // one CTA per tile: the whole scene in natural order, or a segment of
+        // the prepared queue (tiles list[0..count))
         auto *k = checksum ? focus_mixed_staged_kernel<Cfg, true>
                            : focus_mixed_staged_kernel<Cfg, false>;
-        k<<<(unsigned)tiles, Cfg::THREADS, Cfg::smem_bytes, stream>>>(P, map, tb, nt0, o, ctr,
-                                                                       status);
+        k<<<(unsigned)count, Cfg::THREADS, Cfg::smem_bytes, stream>>>(
+            P, map, tb, nt0, queued ? order + first : nullptr, tiles, o, ctr, status);
         return cuda_status(cudaGetLastError(), "focus_mixed_staged launch");
     }
     auto *k = checksum ? focus_mixed_staged_queue_kernel<Cfg, true>
@@ -908,19 +922,12 @@ int launch_staged_t(const SceneParams &P, const MixedLayout &L, char *ws, bool q
                                                                    Cfg::smem_bytes),
                      "queue occupancy");
     if (rc) return rc;
-    if (first < 0 || count < 0 || first + count > tiles || L.ntiles != tiles) {
-        set_error("staged queue: items [%lld, +%lld) outside the %lld-tile queue",
-                  (long long)first, (long long)count, (long long)tiles);
-        return SARBP_EINVAL;
-    }
-    if (count == 0) return SARBP_OK;
     const int64_t grid = std::min<int64_t>(count, (int64_t)std::max(1, per_sm) * sms);
     auto *cursor = reinterpret_cast<unsigned long long *>(ws + L.cursor);
     rc = cuda_status(cudaMemsetAsync(cursor, 0, sizeof(*cursor), stream), "queue cursor reset");
     if (rc) return rc;
     k<<<(unsigned)grid, Cfg::THREADS, Cfg::smem_bytes, stream>>>(
-        P, map, tb, nt0, reinterpret_cast<const int32_t *>(ws + L.vals_out) + first, count,
-        tiles, cursor, o, ctr, status);
+        P, map, tb, nt0, order, count, tiles, cursor, o, ctr, status);
     return cuda_status(cudaGetLastError(), "focus_mixed_staged_queue launch");
 }
 

@@ -184,6 +184,13 @@ def _focus_streamed(args, t: _lib.Tuning, device, blocks: int = STREAM_BLOCKS):
     copy = torch.cuda.Stream(dev)
     copy.wait_stream(compute)               # raw buffer and tables allocated on compute
     scene.raw.record_stream(copy)
+    # segments alternate between two compute streams so that one segment's
+    # last CTAs overlap the next segment's first
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(compute)
+    for tns in (out, ws, scene.raw):
+        tns.record_stream(side)
+    lanes = (compute, side)
     row = scene.pitch * 8
     first = 0
     a0 = 0
@@ -197,14 +204,16 @@ def _focus_streamed(args, t: _lib.Tuning, device, blocks: int = STREAM_BLOCKS):
             scene.h2d_bytes += (hi - lo + 1) * (a1 - a0) * 8
         ev = torch.cuda.Event()
         ev.record(copy)
-        compute.wait_event(ev)
+        lane = lanes[k % 2]
+        lane.wait_event(ev)
         count = int(ends[k]) - first
         if count > 0:
             _lib.check(lib.sarbp_focus_mixed_range(sc, C.byref(tq), out.data_ptr(), None, None,
                                                    None, ws.data_ptr(), ws.numel(), first,
-                                                   count, compute.cuda_stream))
+                                                   count, lane.cuda_stream))
         first = int(ends[k])
         a0 = a1
+    compute.wait_stream(side)
     res = FocusResult(image=out, workspace=ws)
     img = res.to_numpy(scene.dim0, scene.dim1)
     res.check()

@@ -91,9 +91,11 @@ def test_streamed_drop_in_equals_resident_focus(name):
     ref = focus(full, "mixed").check().to_numpy(full.dim0, full.dim1)
     img = FocalizzatoreBpPx(*args, precision="mixed")
     assert focuser.last_call["streamed"]
-    assert np.array_equal(img.view(np.uint64), ref.view(np.uint64))
+    assert np.array_equal(np.ascontiguousarray(img).view(np.uint64),
+                          np.ascontiguousarray(ref).view(np.uint64))
     img1 = FocalizzatoreBpPx(*args, precision="mixed",
                              tuning=dict(chunk=128, tile0=16, tile1=8, staged=1, window=128))
     ref1 = focus(full, "mixed", tuning=dict(chunk=128, tile0=16, tile1=8, staged=1,
                                             window=128)).check().to_numpy(full.dim0, full.dim1)
-    assert np.array_equal(img1.view(np.uint64), ref1.view(np.uint64))
+    assert np.array_equal(np.ascontiguousarray(img1).view(np.uint64),
+                          np.ascontiguousarray(ref1).view(np.uint64))
