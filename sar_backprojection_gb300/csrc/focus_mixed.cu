@@ -342,16 +342,74 @@ int launch_chunk_table(const SceneParams &P, int chunk, int stage, bool paired, 
 
 // Bounds of the range bins a pixel can reach over its aperture, per stage of
 // `stage` pulses as in the staged kernels' window prologue, reduced to one
-// [min, max] for the scene (ints in the status block's spare words).
+// [min, max] for the scene (ints in the status block).  Each block first
+// stages every stage's segment geometry (first pulse, direction, 1/|s|^2,
+// chord deviation) in shared memory; each thread then bounds kBinRangePix
+// pixels from it.
+constexpr int kBinRangePix = 4;
+
 __global__ void raw_bin_range_kernel(const SceneParams P, const PulseFF *__restrict__ pff,
-                                     const float *__restrict__ sdev, int stage, int *range)
+                                     const float *__restrict__ sdev, int stage, int64_t nstages,
+                                     int *range)
+{
+    extern __shared__ float4 geo[];   // [nstages][2]
+    for (int64_t c = threadIdx.x; c < nstages; c += blockDim.x) {
+        const int64_t K = c * stage, kb = min(K + stage - 1, P.naz - 1);
+        const float4 ta = __ldg(&pff[K].hi), tb = __ldg(&pff[kb].hi);
+        const float sx = tb.x - ta.x, sy = tb.y - ta.y, sz = tb.z - ta.z;
+        const float ss = sx * sx + sy * sy + sz * sz;
+        geo[2 * c] = make_float4(ta.x, ta.y, ta.z, ss > 0.f ? 1.0f / ss : 0.f);
+        geo[2 * c + 1] = make_float4(sx, sy, sz, __ldg(&sdev[c]));
+    }
+    __syncthreads();
+    int blo = INT_MAX, bhi = INT_MIN;
+    for (int r = 0; r < kBinRangePix; ++r) {
+        const int64_t ii =
+            ((int64_t)blockIdx.x * kBinRangePix + r) * blockDim.x + threadIdx.x;
+        int64_t lo, hi;
+        if (ii >= P.npix ||
+            !pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi))
+            continue;
+        const PixelFF pf = pixel_ff(P.x[ii], P.y[ii], P.z[ii]);
+        float rmin2 = 3.0e38f, rmax2 = 0.f, dmax = 0.f;
+        for (int64_t c = lo / stage; c <= hi / stage; ++c) {
+            const float4 g0 = geo[2 * c], g1 = geo[2 * c + 1];
+            const float ax = pf.xh - g0.x, ay = pf.yh - g0.y, az = pf.zh - g0.z;
+            const float a2 = ax * ax + ay * ay + az * az;
+            const float d = ax * g1.x + ay * g1.y + az * g1.z;
+            const float u = d * g0.w;
+            const float bx = ax - g1.x, by = ay - g1.y, bz = az - g1.z;
+            const float b2 = bx * bx + by * by + bz * bz;
+            rmin2 = fminf(rmin2, (u > 0.f && u < 1.f) ? fmaf(-d, u, a2) : fminf(a2, b2));
+            rmax2 = fmaxf(rmax2, fmaxf(a2, b2));
+            dmax = fmaxf(dmax, g1.w);
+        }
+        // approximate square roots (relative error ~1e-6) inside the 1-bin margin
+        rmin2 = fmaxf(rmin2, 0.f);
+        const float rmin = rmin2 > 0.f ? rmin2 * rsqrtf(rmin2) : 0.f;
+        const float rmax = rmax2 > 0.f ? rmax2 * rsqrtf(rmax2) : 0.f;
+        blo = min(blo, (int)floorf((rmin - dmax - P.near_hi) * P.inv_dra_f) - 1);
+        bhi = max(bhi, (int)ceilf((rmax + dmax - P.near_hi) * P.inv_dra_f) + 1);
+    }
+    blo = __reduce_min_sync(0xffffffffu, blo);
+    bhi = __reduce_max_sync(0xffffffffu, bhi);
+    if ((threadIdx.x & 31) == 0 && blo <= bhi) {
+        atomicMin(&range[0], blo);
+        atomicMax(&range[1], bhi);
+    }
+}
+
+// The same bound for scenes whose stage table does not fit in shared memory:
+// stage geometry read from the pulse tables, one pixel per thread.
+__global__ void raw_bin_range_gmem_kernel(const SceneParams P, const PulseFF *__restrict__ pff,
+                                          const float *__restrict__ sdev, int stage, int *range)
 {
     const int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int blo = INT_MAX, bhi = INT_MIN;
     int64_t lo, hi;
     if (ii < P.npix && pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi)) {
         const PixelFF pf = pixel_ff(P.x[ii], P.y[ii], P.z[ii]);
-        float rmin = 3.0e38f, rmax = 0.f, dmax = 0.f;
+        float rmin2 = 3.0e38f, rmax2 = 0.f, dmax = 0.f;
         for (int64_t c = lo / stage; c <= hi / stage; ++c) {
             const int64_t K = c * stage, kb = min(K + stage - 1, P.naz - 1);
             const float4 ta = __ldg(&pff[K].hi), tb = __ldg(&pff[kb].hi);
@@ -363,11 +421,11 @@ __global__ void raw_bin_range_kernel(const SceneParams P, const PulseFF *__restr
             const float u = ss > 0.f ? d / ss : 0.f;
             const float bx = ax - sx, by = ay - sy, bz = az - sz;
             const float b2 = bx * bx + by * by + bz * bz;
-            const float rmin2 = (u > 0.f && u < 1.f) ? fmaf(-d, u, a2) : fminf(a2, b2);
-            rmin = fminf(rmin, sqrtf(fmaxf(rmin2, 0.f)));
-            rmax = fmaxf(rmax, sqrtf(fmaxf(a2, b2)));
+            rmin2 = fminf(rmin2, (u > 0.f && u < 1.f) ? fmaf(-d, u, a2) : fminf(a2, b2));
+            rmax2 = fmaxf(rmax2, fmaxf(a2, b2));
             dmax = fmaxf(dmax, __ldg(&sdev[c]));
         }
+        const float rmin = sqrtf(fmaxf(rmin2, 0.f)), rmax = sqrtf(rmax2);
         blo = (int)floorf((rmin - dmax - P.near_hi) * P.inv_dra_f) - 1;
         bhi = (int)ceilf((rmax + dmax - P.near_hi) * P.inv_dra_f) + 1;
     }
@@ -401,12 +459,27 @@ int raw_bin_range(const SceneParams &P, const sarbp_tuning &T, void *workspace, 
     char *ws = static_cast<char *>(workspace);
     int *dr = reinterpret_cast<StatusBlock *>(ws + L.status)->range;
     range_init_kernel<<<1, 1, 0, stream>>>(dr);
-    const int64_t blocks = (P.npix + 255) / 256;
-    if (blocks > 0)
-        raw_bin_range_kernel<<<(unsigned)blocks, 256, 0, stream>>>(
-            P, reinterpret_cast<const PulseFF *>(ws + L.pff),
-            reinterpret_cast<const float *>(ws + L.sdev), T.stage, dr);
-    int rc = cuda_status(cudaGetLastError(), "raw_bin_range launch");
+    const int64_t per_block = 256 * kBinRangePix;
+    const int64_t blocks = (P.npix + per_block - 1) / per_block;
+    const int64_t nstages = (P.naz + T.stage - 1) / T.stage;
+    const size_t smem = sizeof(float4) * 2 * (size_t)nstages;
+    const auto *pff = reinterpret_cast<const PulseFF *>(ws + L.pff);
+    const auto *sdv = reinterpret_cast<const float *>(ws + L.sdev);
+    int rc = SARBP_OK;
+    if (smem <= 200 * 1024) {
+        rc = cuda_status(cudaFuncSetAttribute(raw_bin_range_kernel,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem),
+                         "raw_bin_range smem attribute");
+        if (rc) return rc;
+        if (blocks > 0)
+            raw_bin_range_kernel<<<(unsigned)blocks, 256, smem, stream>>>(P, pff, sdv, T.stage,
+                                                                          nstages, dr);
+    } else if (P.npix > 0) {
+        raw_bin_range_gmem_kernel<<<(unsigned)((P.npix + 255) / 256), 256, 0, stream>>>(
+            P, pff, sdv, T.stage, dr);
+    }
+    rc = cuda_status(cudaGetLastError(), "raw_bin_range launch");
     if (rc) return rc;
     int h[2];
     rc = cuda_status(cudaMemcpyAsync(h, dr, sizeof(h), cudaMemcpyDeviceToHost, stream),
