@@ -153,6 +153,52 @@ def FocalizzatoreBpPx(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
 STREAM_BLOCKS = 8      # pulse blocks of a streamed drop-in upload
 
 
+class _DropIn:
+    """Per-device resources the synchronous drop-in call reuses across calls:
+    its copy and second compute stream and device buffers for the raw rows
+    and the image (a caller's repeated calls then allocate nothing on the
+    device).  The lock serialises calls from several host threads."""
+
+    def __init__(self, dev: torch.device):
+        import threading
+        self.lock = threading.Lock()
+        self.copy = torch.cuda.Stream(dev)
+        self.side = torch.cuda.Stream(dev)
+        self.raw: dict[tuple, torch.Tensor] = {}
+        self.out: dict[int, torch.Tensor] = {}
+
+    def raw_buffer(self, nra: int, naz: int, dev) -> torch.Tensor:
+        key = (naz, nra + (nra & 1))
+        if key not in self.raw:
+            self.raw.clear()                   # one scene shape at a time
+            self.raw[key] = torch.empty((naz, key[1], 2), dtype=torch.float32, device=dev)
+        return self.raw[key]
+
+    def out_buffer(self, npix: int, dev) -> torch.Tensor:
+        if npix not in self.out:
+            self.out.clear()
+            self.out[npix] = torch.empty((npix, 2), dtype=torch.float64, device=dev)
+        return self.out[npix]
+
+
+_dropin: dict = {}
+
+
+def release_drop_in_buffers() -> None:
+    """Free the device buffers the drop-in call keeps between calls."""
+    for r in _dropin.values():
+        with r.lock:
+            r.raw.clear()
+            r.out.clear()
+
+
+def _dropin_for(dev: torch.device) -> _DropIn:
+    key = (dev.type, dev.index)
+    if key not in _dropin:
+        _dropin[key] = _DropIn(dev)
+    return _dropin[key]
+
+
 def _focus_streamed(args, t: _lib.Tuning, device, blocks: int = STREAM_BLOCKS):
     """Drop-in focusing with the raw upload overlapped by focusing.
 
@@ -165,8 +211,17 @@ def _focus_streamed(args, t: _lib.Tuning, device, blocks: int = STREAM_BLOCKS):
     lib = _lib.load()
     tq = _lib.Tuning.from_buffer_copy(t)
     tq.staged = 3
-    scene = scene_to_device(*args, device=device, raw_bins="bound", tuning=tq)
-    dev = scene.device
+    dev = (torch.device(device) if device is not None
+           else torch.device("cuda", torch.cuda.current_device()))
+    res_cache = _dropin_for(dev)
+    with res_cache.lock:
+        return _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache)
+
+
+def _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache: _DropIn):
+    nra, naz = (int(v) for v in tuple(args[8].shape))
+    scene = scene_to_device(*args, device=dev, raw_bins="bound", tuning=tq,
+                            raw_buffer=res_cache.raw_buffer(nra, naz, dev))
     compute = torch.cuda.current_stream(dev)
     sc = C.byref(scene.struct())
     ws = scene.workspace
@@ -175,21 +230,19 @@ def _focus_streamed(args, t: _lib.Tuning, device, blocks: int = STREAM_BLOCKS):
     _lib.check(lib.sarbp_tile_queue_keys(sc, C.byref(tq), ws.data_ptr(), ws.numel(),
                                          keys.ctypes.data_as(C.POINTER(C.c_uint32)), nt,
                                          compute.cuda_stream))
-    out = torch.empty((scene.npix, 2), dtype=torch.float64, device=dev)
+    out = res_cache.out_buffer(scene.npix, dev)
     lo, hi = scene.bin_lo, scene.bin_hi
     naz = scene.naz
     marks = [naz * (k + 1) // blocks for k in range(blocks)]
     ends = np.searchsorted(keys, np.asarray(marks, dtype=np.int64), side="right")
     ends[-1] = nt
-    copy = torch.cuda.Stream(dev)
+    copy = res_cache.copy
     copy.wait_stream(compute)               # raw buffer and tables allocated on compute
-    scene.raw.record_stream(copy)
     # segments alternate between two compute streams so that one segment's
     # last CTAs overlap the next segment's first
-    side = torch.cuda.Stream(dev)
+    side = res_cache.side
     side.wait_stream(compute)
-    for tns in (out, ws, scene.raw):
-        tns.record_stream(side)
+    ws.record_stream(side)
     lanes = (compute, side)
     row = scene.pitch * 8
     first = 0

@@ -193,7 +193,8 @@ def _upload_reached_bins(scene: "DeviceScene", host_rows: torch.Tensor, upload: 
 
 def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
                     near_range, dra, lambda_val, Sint, device=None,
-                    raw_bins: str = "all", tuning=None) -> DeviceScene:
+                    raw_bins: str = "all", tuning=None,
+                    raw_buffer: torch.Tensor | None = None) -> DeviceScene:
     """Upload the reference's 13 focusing arguments (same order) to the device.
 
     Raises ValueError where the reference does (Raw_Data or xxg1 not 2-D,
@@ -209,6 +210,9 @@ def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
     whole.  ``raw_bins="bound"``: the same bound, but no raw row is copied
     (the caller streams them; ``scene.host_rows`` is the host source) and
     ``scene.workspace`` holds tables prepared with ``tuning``.
+    ``raw_buffer``: a float32 (Naz, pitch, 2) device tensor to receive the
+    raw rows in those two modes instead of a new allocation (the caller owns
+    its reuse).
     """
     if raw_bins not in ("all", "reached", "bound"):
         raise ValueError(f"raw_bins must be 'all', 'reached' or 'bound', got {raw_bins!r}")
@@ -236,7 +240,11 @@ def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
     host_rows = _pulse_major_host(Raw_Data) if raw_bins != "all" else None
     if host_rows is not None:
         pitch = nra + (nra & 1)
-        raw_t = torch.empty((naz, pitch, 2), dtype=torch.float32, device=device)
+        if (raw_buffer is not None and tuple(raw_buffer.shape) == (naz, pitch, 2)
+                and raw_buffer.dtype == torch.float32 and raw_buffer.device == device):
+            raw_t = raw_buffer
+        else:
+            raw_t = torch.empty((naz, pitch, 2), dtype=torch.float32, device=device)
     else:
         raw_t, nra, naz, pitch = raw_to_device(Raw_Data, device)
 
