@@ -343,6 +343,10 @@ def run_serving(args, dev):
         raw.copy_(sc["RawData"].t())
         args13 = list(synth.focus_args(sc))
         args13[8] = raw.t()
+        for i in (0, 1, 2, 3, 4, 5, 6, 7, 12):       # DEM, masks, trajectory: pinned too
+            a = np.asarray(args13[i])
+            t = torch.from_numpy(np.ascontiguousarray(a.T) if a.ndim == 2 else a)
+            args13[i] = t.pin_memory().t() if a.ndim == 2 else t.pin_memory()
         pool.append(tuple(args13))
     rng = np.random.default_rng(11)
     picks = rng.integers(0, len(pool), args.serve_jobs)

@@ -4,6 +4,7 @@ Requests (focusing jobs of different sizes) arrive over time.  The engine
 
 * admits a waiting job as soon as a scene slot and enough of the HBM budget
   are free, uploading its inputs on a copy stream while other jobs' work runs
+  -- of host raw data only the range bins the job's apertures can reach
   (the job's raw data and trajectory then stay resident until it finishes);
 * runs the device in *waves*: each wave is one launch of the persistent
   batch kernel whose work queue holds pixel tiles of every admitted job, so a
@@ -134,14 +135,21 @@ class ServingEngine:
         slot = self.free_slots.pop(0)
         tb = C.byref(self.tuning)
         with torch.cuda.stream(self.copy):
-            scene = scene_to_device(*job.args, device=self.device)
+            # host raw data in the reference's layout: only the range bins the
+            # job's apertures can reach go up (the bound is computed on the
+            # copy stream, which is all the admission synchronises)
+            scene = scene_to_device(*job.args, device=self.device, raw_bins="reached",
+                                    tuning=self.tuning)
             ws_bytes = _lib.check(int(self.lib.sarbp_mixed_workspace_size(
                 C.byref(scene.struct()), tb)))
-            ws = torch.empty(ws_bytes, dtype=torch.uint8, device=self.device)
             out = torch.empty((scene.npix, 2), dtype=torch.float64, device=self.device)
             sp = self.copy.cuda_stream
-            _lib.check(self.lib.sarbp_mixed_prepare(C.byref(scene.struct()), tb,
-                                                    ws.data_ptr(), ws_bytes, sp))
+            if scene.workspace is not None and scene.workspace.numel() >= ws_bytes:
+                ws = scene.workspace            # prepared with this tuning on the way
+            else:
+                ws = torch.empty(ws_bytes, dtype=torch.uint8, device=self.device)
+                _lib.check(self.lib.sarbp_mixed_prepare(C.byref(scene.struct()), tb,
+                                                        ws.data_ptr(), ws_bytes, sp))
             nt = _lib.check(int(self.lib.sarbp_tile_count(C.byref(scene.struct()), tb)))
             for b in self.bws:
                 _lib.check(self.lib.sarbp_batch_set_scene(
