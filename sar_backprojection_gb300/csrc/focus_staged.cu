@@ -214,30 +214,36 @@ int tile_costs(const SceneParams &P, const sarbp_tuning &T, int64_t *costs, cuda
 
 // Queue key of each tile: its estimated cost (sum of its pixels' kept
 // aperture lengths) or, with kEnd, one past its last kept pulse (0 for a tile
-// without apertures).
+// without apertures).  One warp per tile, lanes over its pixels.
 template <int T0, int T1, bool kEnd>
 __global__ void tile_key_kernel(const SceneParams P, int64_t ntile0, int64_t ntiles,
                                 uint32_t *__restrict__ keys, int32_t *__restrict__ ids)
 {
-    const int64_t tile = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tile >= ntiles) return;
+    const int64_t tile = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (tile >= ntiles) return;              // warp-uniform
     const int64_t t0 = tile % ntile0, t1 = tile / ntile0;
-    uint64_t c = 0;
-    for (int b = 0; b < T1; ++b)
-        for (int a = 0; a < T0; ++a) {
-            const int64_t i0 = t0 * T0 + a, i1 = t1 * T1 + b;
-            if (i0 >= P.dim0 || i1 >= P.dim1) continue;
-            const int64_t ii = i0 + P.dim0 * i1;
-            int64_t lo, hi;
-            if (pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi)) {
-                if (kEnd)
-                    c = c > (uint64_t)(hi + 1) ? c : (uint64_t)(hi + 1);
-                else
-                    c += (uint64_t)(hi - lo + 1);
-            }
+    unsigned long long c = 0;
+    for (int p = lane; p < T0 * T1; p += 32) {
+        const int64_t i0 = t0 * T0 + p % T0, i1 = t1 * T1 + p / T0;
+        if (i0 >= P.dim0 || i1 >= P.dim1) continue;
+        const int64_t ii = i0 + P.dim0 * i1;
+        int64_t lo, hi;
+        if (pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi)) {
+            if (kEnd)
+                c = c > (unsigned long long)(hi + 1) ? c : (unsigned long long)(hi + 1);
+            else
+                c += (unsigned long long)(hi - lo + 1);
         }
-    keys[tile] = c > 0xffffffffull ? 0xffffffffu : (uint32_t)c;
-    ids[tile] = (int32_t)tile;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long v = __shfl_xor_sync(0xffffffffu, c, o);
+        c = kEnd ? (c > v ? c : v) : c + v;
+    }
+    if (lane == 0) {
+        keys[tile] = c > 0xffffffffull ? 0xffffffffu : (uint32_t)c;
+        ids[tile] = (int32_t)tile;
+    }
 }
 
 size_t tile_sort_bytes(int64_t ntiles)
@@ -268,16 +274,16 @@ int tile_order(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L
     const int64_t nt0 = (P.dim0 + T.tile0 - 1) / T.tile0;
     auto *keys_in = reinterpret_cast<uint32_t *>(ws + L.keys_in);
     auto *vals_in = reinterpret_cast<int32_t *>(ws + L.vals_in);
-    const unsigned blocks = (unsigned)((nt + 127) / 128);
+    const unsigned blocks = (unsigned)((nt + 7) / 8);   // 8 warps (tiles) per block
     const bool by_end = T.staged == 3;
     bool launched = false;
 #define X(A, B)                                                                             \
     if (!launched && T.tile0 == A && T.tile1 == B) {                                        \
         if (by_end)                                                                         \
-            tile_key_kernel<A, B, true><<<blocks, 128, 0, stream>>>(P, nt0, nt, keys_in,    \
+            tile_key_kernel<A, B, true><<<blocks, 256, 0, stream>>>(P, nt0, nt, keys_in,    \
                                                                     vals_in);               \
         else                                                                                \
-            tile_key_kernel<A, B, false><<<blocks, 128, 0, stream>>>(P, nt0, nt, keys_in,   \
+            tile_key_kernel<A, B, false><<<blocks, 256, 0, stream>>>(P, nt0, nt, keys_in,   \
                                                                      vals_in);              \
         launched = true;                                                                    \
     }
