@@ -32,7 +32,11 @@ namespace sarbp {
 constexpr float kUMax = 4.0e-3f;      // series validity bound on |D|/R0^2
 constexpr float kDRMax = 16.0f;       // metres; keeps |dphi| small in FP32
 // Tie band: |fr| > 0.5 - eps, eps = kEpsRel*|dR|max/dra + kEpsAbs, where
-// 6e-7*|dR|max/dra + 1e-6 bounds the FP32 error of g.
+// 6e-7*|dR|max/dra + 1e-6 bounds the FP32 error of g: the roundings of the
+// FP32 products -2*d0.e and |e|^2 (relative 2^-24 of terms up to |D|), the
+// three FMAs of D, the series (its truncation < 4e-8 m at |u| <= 4e-3) and
+// the FP32 1/dra, each a relative error of a few 2^-24 of dR/dra, plus the
+// float-float reference g0 (< 1e-9 bin).
 constexpr float kEpsRel = 1.5e-6f;
 constexpr float kEpsAbs = 2.0e-6f;
 

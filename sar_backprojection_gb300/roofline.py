@@ -1,4 +1,4 @@
-"""Roofline constants of the back-projection path (frozen).
+"""Roofline constants of the back-projection path (frozen: bench lines stay comparable).
 
 Unit of work: one nominal pixel-pulse back-projection = one (pixel, pulse)
 pair of an unmasked pixel's aperture, ``sum over pixels with mask == 1 and
