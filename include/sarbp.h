@@ -295,6 +295,33 @@ SARBP_API int sarbp_focus_mixed_noalloc(const sarbp_scene *scene,
                                         void *stream);
 
 /*
+ * Serving queue: continuous batching of focusing jobs on one device.
+ * sarbp_queue_create starts a worker thread on the calling thread's current
+ * device with two streams and two batch workspaces (`max_slots` scenes
+ * resident at once, waves of up to `wave_items` tiles; 0 picks 6 per SM;
+ * tuning.staged must be 1).  sarbp_queue_submit enqueues a device-resident
+ * scene (caller-owned buffers, valid until the job is done) with its device
+ * output (npix complex128) and returns a job id (>= 0) or a negative status.
+ * The worker admits jobs into free slots in arrival order and runs waves of
+ * the persistent batch kernel over the tiles of every admitted job; a job's
+ * image equals sarbp_focus_mixed's bit for bit.  sarbp_queue_poll returns 1
+ * when the job is done, 0 while it is not, a negative status if it failed
+ * (SARBP_ETIMEOUT when a bounded device wait gave up); sarbp_queue_wait
+ * blocks until done.  Completion is reported once: the job id is released
+ * then.  sarbp_queue_destroy finishes the submitted jobs, stops the worker
+ * and frees the queue.  Replaces the reference's per-batch host loops
+ * (gpu_small_dataset.py:285-339) for many independent requests; the
+ * reference has no serving component.
+ */
+typedef struct sarbp_queue sarbp_queue;
+SARBP_API int sarbp_queue_create(sarbp_queue **queue, const sarbp_tuning *tuning,
+                                 int32_t max_slots, int64_t wave_items);
+SARBP_API int64_t sarbp_queue_submit(sarbp_queue *queue, const sarbp_scene *scene, double *out);
+SARBP_API int sarbp_queue_poll(sarbp_queue *queue, int64_t job);
+SARBP_API int sarbp_queue_wait(sarbp_queue *queue, int64_t job);
+SARBP_API int sarbp_queue_destroy(sarbp_queue *queue);
+
+/*
  * Measurement helper (no counterpart in the reference, which publishes no
  * roofline): measures this device's issue rates with probe kernels on
  * `stream` and returns them in rates[0..3] = FP32 FMA lanes/s, SFU sin

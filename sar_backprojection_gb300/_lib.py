@@ -76,6 +76,12 @@ SIGNATURES = {
                                              _P, _P, C.c_size_t, _P]),
     "sarbp_probe_issue_rates": (C.c_int, [C.POINTER(C.c_double), _P]),
     "sarbp_mixed_status": (C.c_int, [_P, C.c_size_t, _P]),
+    "sarbp_queue_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(Tuning), C.c_int32,
+                                     C.c_int64]),
+    "sarbp_queue_submit": (C.c_int64, [_P, C.POINTER(Scene), _P]),
+    "sarbp_queue_poll": (C.c_int, [_P, C.c_int64]),
+    "sarbp_queue_wait": (C.c_int, [_P, C.c_int64]),
+    "sarbp_queue_destroy": (C.c_int, [_P]),
     "sarbp_tile_queue_keys": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, C.c_size_t,
                                         C.POINTER(C.c_uint32), C.c_int64, _P]),
     "sarbp_focus_mixed_range": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, _P, _P, _P,

@@ -324,3 +324,53 @@ def run_fp64_sequential(jobs: list[Job], device=None) -> dict:
     lat = np.array(lat) * 1e3
     return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "busy_s": busy, "pixel_pulses": work, "gpix_pulse_per_s": work / busy / 1e9}
+
+
+class NativeQueue:
+    """The C serving queue (sarbp_queue_*): device-resident scenes in, device
+    images out; a native worker thread admits them and runs waves of the
+    persistent batch kernel.  ``submit`` returns a job id; ``wait``/``poll``
+    report completion (once per job)."""
+
+    def __init__(self, tuning=None, max_slots: int = 32, wave_items: int = 0):
+        self.lib = _lib.load()
+        self.tuning = staged_tuning() if tuning is None else resolve_tuning(tuning)
+        self._q = C.c_void_p()
+        _lib.check(self.lib.sarbp_queue_create(C.byref(self._q), C.byref(self.tuning),
+                                               int(max_slots), int(wave_items)))
+        self._keep: dict[int, tuple] = {}
+
+    def submit(self, scene: DeviceScene, out: torch.Tensor | None = None) -> int:
+        if out is None:
+            out = torch.empty((scene.npix, 2), dtype=torch.float64, device=scene.device)
+        # inputs must be on the device before the worker's streams read them
+        torch.cuda.current_stream(scene.device).synchronize()
+        job = _lib.check(int(self.lib.sarbp_queue_submit(self._q, C.byref(scene.struct()),
+                                                         out.data_ptr())))
+        self._keep[job] = (scene, out)
+        return job
+
+    def poll(self, job: int) -> bool:
+        done = _lib.check(int(self.lib.sarbp_queue_poll(self._q, job))) == 1
+        return done
+
+    def wait(self, job: int) -> torch.Tensor:
+        """Block until the job is done; its (npix, 2) float64 device image."""
+        try:
+            _lib.check(int(self.lib.sarbp_queue_wait(self._q, job)))
+        finally:
+            scene, out = self._keep.pop(job, (None, None))
+        return out
+
+    def close(self) -> None:
+        if self._q:
+            rc = int(self.lib.sarbp_queue_destroy(self._q))
+            self._q = C.c_void_p()
+            self._keep.clear()
+            _lib.check(rc)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
