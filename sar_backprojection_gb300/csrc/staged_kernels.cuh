@@ -54,10 +54,10 @@ constexpr int kMaxTileThreads = 256;       // pixels (threads) per tile
 constexpr uint32_t kWaitLimit = 1u << 22;  // mbarrier polls before giving up
 
 // Compile-time shape of a staged variant.
-template <int CHUNK_, int T0_, int T1_, int W_, int STAGE_>
+template <int CHUNK_, int T0_, int T1_, int W_, int STAGE_, int NBUF_>
 struct StagedCfg {
     static constexpr int CHUNK = CHUNK_, T0 = T0_, T1 = T1_, W = W_, STAGE = STAGE_;
-    static constexpr int NBUF = 64 / STAGE;        // 64 pulses of raw windows in flight
+    static constexpr int NBUF = NBUF_;             // ring buffers (raw windows in flight)
     static constexpr int R = CHUNK / STAGE;        // stages per chunk
     static constexpr int THREADS = T0 * T1, WARPS = THREADS / 32;
     static constexpr size_t raw_bytes = (size_t)STAGE * W * sizeof(float2);
@@ -65,7 +65,12 @@ struct StagedCfg {
     static constexpr size_t buf_bytes = raw_bytes + tab_bytes;
     static constexpr size_t smem_bytes = NBUF * buf_bytes + 128;   // + alignment slack
     static_assert(STAGE == 16 || STAGE == 32, "stage");
-    static_assert(NBUF <= kMaxBuf && (NBUF & (NBUF - 1)) == 0, "ring");
+    static_assert(NBUF >= 2 && NBUF <= kMaxBuf, "ring");
+    // tile-start lane keys and the prologue's stage geometry live at the
+    // start of the (then idle) ring buffers
+    static_assert(NBUF * buf_bytes >= 8 * kMaxTileThreads &&
+                      NBUF * buf_bytes >= 32 * kMaxPassStages,
+                  "scratch aliases");
     static_assert(CHUNK % STAGE == 0 && kMaxPassStages % R == 0, "chunk");
     static_assert(buf_bytes % 128 == 0, "TMA destinations stay 128-byte aligned");
     static_assert(THREADS <= kMaxTileThreads && (THREADS & (THREADS - 1)) == 0, "tile");
@@ -182,9 +187,6 @@ struct StagedShared {
     int issued[kMaxBuf];              // a copy was ever issued into the buffer
     int stop;                         // a bounded wait gave up
     int wlo[kMaxPassStages], whi[kMaxPassStages];   // range windows of a pass
-    float4 geo[kMaxPassStages][2];    // per stage: first pulse t(K) (hi parts) and
-                                      // s = t(K+STAGE-1) - t(K); 1/|s|^2, chord deviation
-    unsigned long long lane_key[kMaxTileThreads];   // lane assignment sort
     long long lo, hi;                 // tile-wide pulse range
     long long item[2];                // persistent kernels: current work item
     float2 zero;                      // read by masked-off pulses of the fast path
@@ -252,12 +254,15 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
     // Pixels without an aperture (masked, outside the DEM) gather in the last
     // warps, which then skip every stage, and each warp's apertures start and
     // end close together, so more of its stages take the fast path.
-    sh.lane_key[t] = ((unsigned long long)(active ? (uint32_t)(lo + hi) : 0xffffffffu) << 16) |
+    // scratch in the ring buffers, idle between tiles (no copy in flight)
+    unsigned long long *lane_key = reinterpret_cast<unsigned long long *>(smem);
+    lane_key[t] = ((unsigned long long)(active ? (uint32_t)(lo + hi) : 0xffffffffu) << 16) |
                      (unsigned)t;
     __syncthreads();
-    cta_bitonic_sort<Cfg::THREADS>(sh.lane_key, t);
+    cta_bitonic_sort<Cfg::THREADS>(lane_key, t);
     {
-        const int src = (int)(sh.lane_key[t] & 0xffffu);
+        const int src = (int)(lane_key[t] & 0xffffu);
+        __syncthreads();                       // keys read before the buffers are reused
         staged_tile_pixel<Cfg::T0, Cfg::T1>(src, tile0, tile1, i0, i1);
         inside = i0 < P.dim0 && i1 < P.dim1;
         ii = inside ? i0 + P.dim0 * i1 : 0;
@@ -298,15 +303,17 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
         for (int64_t cb = c_first; cb <= c_last && !stopped; cb += kMaxPassStages) {
             const int npass = (int)min((int64_t)kMaxPassStages, c_last - cb + 1);
             // ---- window prologue: bins every pixel can reach per stage ----
-            // stage geometry of the pass into shared memory (one stage per thread)
+            // stage geometry of the pass into shared memory (one stage per
+            // thread), in the ring buffers: no copy is in flight yet
+            float4 *geo = reinterpret_cast<float4 *>(smem);
             for (int q = t; q < npass; q += blockDim.x) {
                 const int64_t K = (cb + q) * STAGE;
                 const int64_t kb = min(K + STAGE - 1, P.naz - 1);
                 const float4 ta = __ldg(&pff[K].hi), tb = __ldg(&pff[kb].hi);
                 const float sx = tb.x - ta.x, sy = tb.y - ta.y, sz = tb.z - ta.z;
                 const float ss = sx * sx + sy * sy + sz * sz;
-                sh.geo[q][0] = make_float4(ta.x, ta.y, ta.z, ss > 0.f ? 1.0f / ss : 0.f);
-                sh.geo[q][1] = make_float4(sx, sy, sz, __ldg(&sdev[cb + q]));
+                geo[2 * q] = make_float4(ta.x, ta.y, ta.z, ss > 0.f ? 1.0f / ss : 0.f);
+                geo[2 * q + 1] = make_float4(sx, sy, sz, __ldg(&sdev[cb + q]));
                 sh.wlo[q] = INT_MAX;
                 sh.whi[q] = INT_MIN;
             }
@@ -320,7 +327,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                     // endpoints (max), closest point (min), widened by the
                     // chord deviation; approximate square roots (relative
                     // error ~1e-6, ~4 mm at 4 km) inside the 1-bin margin
-                    const float4 g0 = sh.geo[q][0], g1 = sh.geo[q][1];
+                    const float4 g0 = geo[2 * q], g1 = geo[2 * q + 1];
                     const float ax = pf.xh - g0.x, ay = pf.yh - g0.y, az = pf.zh - g0.z;
                     const float a2 = ax * ax + ay * ay + az * az;
                     const float d = ax * g1.x + ay * g1.y + az * g1.z;
@@ -366,10 +373,13 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
             };
             const uint32_t it0 = cta.it;
             // every buffer is free at a pass start: prime the ring (a
-            // diagnostic withhold leaves stage 0 uncopied: its wait runs out)
-            if (t == 0)
+            // diagnostic withhold leaves stage 0 uncopied: its wait runs out);
+            // the copies overwrite the scratch the barrier above retired
+            if (t == 0) {
+                fence_proxy_async_smem();
                 for (int q = P.withhold ? 1 : 0; q < NBUF && q < npass; ++q)
                     issue(q, (int)((it0 + q) % NBUF), (it0 + q) / NBUF);
+            }
 
             for (int q = 0; q < npass; ++q) {
                 const uint32_t itq = it0 + (uint32_t)q;
@@ -961,8 +971,9 @@ int launch_batch_t(char *bws, const BatchLayout &BL, int64_t n_items, bool diag,
 // instantiated in staged_c32.cu / staged_c64.cu / staged_c128.cu.
 // SARBP_EINVAL (with a message) for a variant that is not built.
 #define SARBP_STAGED_TILES(X, C)                                                            \
-    X(C, 16, 16, 160, 32) X(C, 16, 16, 160, 16) X(C, 16, 16, 128, 32) X(C, 16, 8, 128, 32)   \
-    X(C, 16, 8, 128, 16) X(C, 32, 8, 128, 32) X(C, 64, 4, 128, 32)
+    X(C, 16, 16, 160, 32, 2) X(C, 16, 16, 160, 16, 4) X(C, 16, 16, 144, 32, 3)              \
+    X(C, 16, 16, 136, 32, 3) X(C, 16, 16, 128, 32, 2) X(C, 16, 8, 128, 32, 2)               \
+    X(C, 16, 8, 128, 16, 4) X(C, 32, 8, 128, 32, 2) X(C, 64, 4, 128, 32, 2)
 
 template <int C>
 int launch_staged_chunk(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L,
@@ -970,9 +981,9 @@ int launch_staged_chunk(const SceneParams &P, const sarbp_tuning &T, const Mixed
                         int32_t *nvalid, uint64_t *checksum, uint64_t *counters,
                         cudaStream_t stream)
 {
-#define X(C_, A, B, W, S)                                                                   \
+#define X(C_, A, B, W, S, NB)                                                               \
     if (T.tile0 == A && T.tile1 == B && T.window == W && T.stage == S)                      \
-        return launch_staged_t<StagedCfg<C_, A, B, W, S>>(P, L, ws, queued, first, count,   \
+        return launch_staged_t<StagedCfg<C_, A, B, W, S, NB>>(P, L, ws, queued, first, count, \
                                                           out, nvalid, checksum, counters,  \
                                                           stream);
     SARBP_STAGED_TILES(X, C)
@@ -986,9 +997,9 @@ template <int C>
 int launch_batch_chunk(char *bws, const BatchLayout &BL, const sarbp_tuning &T, int64_t n_items,
                        bool diag, uint64_t *counters, cudaStream_t stream)
 {
-#define X(C_, A, B, W, S)                                                                   \
+#define X(C_, A, B, W, S, NB)                                                               \
     if (T.tile0 == A && T.tile1 == B && T.window == W && T.stage == S)                      \
-        return launch_batch_t<StagedCfg<C_, A, B, W, S>>(bws, BL, n_items, diag, counters,  \
+        return launch_batch_t<StagedCfg<C_, A, B, W, S, NB>>(bws, BL, n_items, diag, counters, \
                                                          stream);
     SARBP_STAGED_TILES(X, C)
 #undef X
