@@ -296,18 +296,20 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
     safe_setup(S, 0);
     StageCoef C = stage_coef(S);
     bool gwork = false;                   // pixel has pulses in the current chunk
-    int64_t cur_chunk = -1;
+    int cur_chunk = -1;
+    // pulse indices fit 32 bits (launches check naz < 2^31)
+    const int lo32 = (int)lo, hi32 = (int)hi;
     float gre = 0.f, gim = 0.f;           // FP32 partial sum of the current chunk
     if (thi >= 0) {
-        const int64_t c_first = tlo / STAGE, c_last = thi / STAGE;
-        for (int64_t cb = c_first; cb <= c_last && !stopped; cb += kMaxPassStages) {
-            const int npass = (int)min((int64_t)kMaxPassStages, c_last - cb + 1);
+        const int c_first = (int)(tlo / STAGE), c_last = (int)(thi / STAGE);
+        for (int cb = c_first; cb <= c_last && !stopped; cb += kMaxPassStages) {
+            const int npass = min(kMaxPassStages, c_last - cb + 1);
             // ---- window prologue: bins every pixel can reach per stage ----
             // stage geometry of the pass into shared memory (one stage per
             // thread), in the ring buffers: no copy is in flight yet
             float4 *geo = reinterpret_cast<float4 *>(smem);
             for (int q = t; q < npass; q += blockDim.x) {
-                const int64_t K = (cb + q) * STAGE;
+                const int64_t K = (int64_t)(cb + q) * STAGE;
                 const int64_t kb = min(K + STAGE - 1, P.naz - 1);
                 const float4 ta = __ldg(&pff[K].hi), tb = __ldg(&pff[kb].hi);
                 const float sx = tb.x - ta.x, sy = tb.y - ta.y, sz = tb.z - ta.z;
@@ -349,14 +351,22 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                 }
             }
             __syncthreads();
+            // per stage: TMA start bin (even: 16-byte aligned x coordinate,
+            // inside [0, nra]; 0 for a stage no pixel reaches) into wlo, and
+            // into whi whether the window covers every reachable bin and lies
+            // inside the kept bins 0..nra-2 (no per-pulse tests then)
+            for (int q = t; q < npass; q += blockDim.x) {
+                const int wl = sh.wlo[q], wh = sh.whi[q];
+                const int b0 = wl > wh ? 0 : (int)min((int64_t)max(wl, 0), P.nra) & ~1;
+                const bool ok = wl <= wh && wl >= 0 && (int64_t)wh <= P.nra - 2 && wh - b0 < W;
+                sh.wlo[q] = b0;
+                sh.whi[q] = ok ? 1 : 0;
+            }
+            __syncthreads();
 
             // window start of stage q: even (16-byte aligned TMA x coordinate),
             // inside [0, nra]; 0 for a stage no pixel of the tile reaches
-            auto window_start = [&](int q) {
-                const int wl = sh.wlo[q], wh = sh.whi[q];
-                if (wl > wh) return 0;
-                return (int)min((int64_t)max(wl, 0), P.nra) & ~1;
-            };
+            auto window_start = [&](int q) { return sh.wlo[q]; };
             // copies of stage q of this pass into buffer b (any single thread)
             auto issue = [&](int q, int b, uint32_t use) {
                 unsigned char *base = smem + (size_t)b * Cfg::buf_bytes;
@@ -385,14 +395,14 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                 const uint32_t itq = it0 + (uint32_t)q;
                 const int b = (int)(itq % NBUF);
                 const uint32_t use = itq / NBUF;
-                const int64_t c = cb + q;
-                const int64_t K = c * STAGE;
+                const int c = cb + q;
+                const int K = c * STAGE;
                 // ---- chunk reference: once per CHUNK pulses, before the wait ----
-                const int64_t chunk = c / R;
+                const int chunk = c / R;
                 if (chunk != cur_chunk) {
                     cur_chunk = chunk;
-                    const int64_t C0 = chunk * CHUNK;
-                    gwork = active && lo <= C0 + CHUNK - 1 && hi >= C0;
+                    const int C0 = chunk * CHUNK;
+                    gwork = active && lo32 <= C0 + CHUNK - 1 && hi32 >= C0;
                     gre = gim = 0.f;
                     if (gwork) {
                         ++chunks;
@@ -412,18 +422,15 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                     stopped = true;
                     break;
                 }
-                const int jmin = (int)(lo > K ? lo - K : 0);
-                const int jmax = (int)(hi < K + STAGE - 1 ? hi - K : STAGE - 1);
+                const int jmin = lo32 > K ? lo32 - K : 0;
+                const int jmax = hi32 < K + STAGE - 1 ? hi32 - K : STAGE - 1;
                 const bool work = gwork && jmin <= jmax;
                 const float2 *sraw =
                     reinterpret_cast<const float2 *>(smem + (size_t)b * Cfg::buf_bytes);
                 const float4 *stab = reinterpret_cast<const float4 *>(
                     smem + (size_t)b * Cfg::buf_bytes + Cfg::raw_bytes);
                 const int b0 = window_start(q);
-                // window covers every bin the tile can reach and lies inside
-                // the kept bins 0..nra-2: no per-pulse validity/window tests
-                const bool win_ok = sh.wlo[q] >= 0 && (int64_t)sh.whi[q] <= P.nra - 2 &&
-                                    sh.whi[q] - b0 < W;
+                const bool win_ok = sh.whi[q] != 0;
                 const bool exact = work && S.exact;
                 // fast path: the window holds every bin the warp's pixels can
                 // reach; pulses outside a lane's aperture are masked off
