@@ -594,8 +594,12 @@ def run_ours(args, dist: Dist):
                "p99_ms": 1e3 * float(np.percentile(ts, 99)),
                "what": "single-scene drop-in call latency (host inputs to host image)"}
 
-    batch_res = run_batch(args, dev, tuning) if args.batch_scenes > 0 else None
-    serving_res = run_serving(args, dev) if args.serve_jobs > 0 else None
+    # the batched and serving measurements describe one GPU: rank 0 runs them
+    # (under torchrun the other ranks' GPUs are then idle, and their host
+    # memory is not pinned for the serving pool)
+    batch_res = (run_batch(args, dev, tuning)
+                 if args.batch_scenes > 0 and dist.rank == 0 else None)
+    serving_res = run_serving(args, dev) if args.serve_jobs > 0 and dist.rank == 0 else None
 
     cpu = None
     if not args.no_cpu_baseline and dist.rank == 0:

@@ -110,3 +110,48 @@ def test_workspace_size_is_host_only():
     t.wait_polls = 0
     t.chunk = 48
     assert lib.sarbp_mixed_workspace_size(C.byref(s), C.byref(t)) == _lib.SARBP_EINVAL
+
+
+def test_new_entry_points_reject_bad_arguments_without_a_gpu():
+    """Argument checks of the upload, bound, queue-range and serving-queue
+    entry points run on the host and never touch a device."""
+    lib = _lib.load()
+    # upload of a bin range that does not fit the rows
+    assert lib.sarbp_upload_raw_bins(C.c_void_p(0x1000), 100, C.c_void_p(0x2000), 100, 90, 20,
+                                     5, None) == _lib.SARBP_EINVAL
+    assert "bin range" in _lib.last_error()
+    assert lib.sarbp_upload_raw_bins(None, 100, C.c_void_p(0x2000), 100, 0, 10, 5,
+                                     None) == _lib.SARBP_EINVAL
+    # zero bins or pulses: nothing to do
+    assert lib.sarbp_upload_raw_bins(C.c_void_p(0x1000), 100, C.c_void_p(0x2000), 100, 0, 0,
+                                     5, None) == _lib.SARBP_OK
+    s = _lib.Scene()
+    s.dim0, s.dim1 = 64, 16
+    for f in ("dem_x", "dem_y", "dem_z", "mask", "index", "sint", "traj_x", "traj_y",
+              "traj_z", "raw"):
+        setattr(s, f, 0x1000)
+    s.nra, s.naz, s.raw_pitch = 512, 1201, 512
+    s.delta_range, s.lambda_, s.near_range = 0.5, 0.031, 3500.0
+    t = _lib.default_tuning()
+    rng = (C.c_int64 * 2)()
+    # bound without a workspace
+    assert lib.sarbp_raw_bin_range(C.byref(s), C.byref(t), None, 0, rng,
+                                   None) == _lib.SARBP_EWORKSPACE
+    # queue range / keys need a queued tuning
+    out = C.c_void_p(0x3000)
+    assert lib.sarbp_focus_mixed_range(C.byref(s), C.byref(t), out, None, None, None,
+                                       C.c_void_p(0x4000), 1 << 30, 0, 4,
+                                       None) == _lib.SARBP_EINVAL
+    keys = (C.c_uint32 * 4)()
+    t.staged = 3
+    assert lib.sarbp_tile_queue_keys(C.byref(s), C.byref(t), None, 0, keys, 4,
+                                     None) == _lib.SARBP_EWORKSPACE
+    # serving queue: bad sizes, a non-batch tuning, and a NULL destroy
+    q = C.c_void_p()
+    assert lib.sarbp_queue_create(C.byref(q), None, 0, 0) == _lib.SARBP_EINVAL
+    t2 = _lib.default_tuning()
+    t2.staged = 2
+    assert lib.sarbp_queue_create(C.byref(q), C.byref(t2), 4, 0) == _lib.SARBP_EINVAL
+    assert "staged = 1" in _lib.last_error()
+    assert lib.sarbp_queue_submit(None, C.byref(s), out) == _lib.SARBP_EINVAL
+    assert lib.sarbp_queue_destroy(None) == _lib.SARBP_OK
