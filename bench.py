@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tuning", type=str, default="",
@@ -378,8 +378,8 @@ def run_serving(args, dev):
 
 TUNING_FIELDS = ("chunk", "tile0", "tile1", "staged", "window", "stage")
 # staged-kernel variants timed on the workload itself; the fastest is measured
-AUTOTUNE_CANDIDATES = ((64, 16, 16, 1, 160, 32), (128, 16, 16, 1, 160, 32),
-                       (32, 16, 16, 1, 160, 32), (128, 16, 8, 1, 128, 32))
+AUTOTUNE_CANDIDATES = ((64, 16, 16, 1, 208, 32), (128, 16, 16, 1, 208, 32),
+                       (128, 16, 16, 1, 192, 32), (128, 16, 16, 1, 160, 32))
 
 
 def pick_tuning(lib, ds, dev, candidates=AUTOTUNE_CANDIDATES, reps: int = 5):
@@ -559,7 +559,7 @@ def run_ours(args, dist: Dist):
                 host["wgsx"], host["wgsy"], host["wgsz"], host["RawData"],
                 float(scene["NearRange"]), float(scene["DeltaRange"]), float(scene["Lambda"]),
                 host["Sint"])
-        for _ in range(3):
+        for _ in range(5):
             FocalizzatoreBpPx(*argv, precision="mixed", tuning=tuning, device=dev)
         torch.cuda.synchronize(dev)
         dist.barrier()
@@ -584,6 +584,7 @@ def run_ours(args, dist: Dist):
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "ms_per_step": 1e3 * e2e_s, "api": "FocalizzatoreBpPx(..., precision='mixed')",
                "raw_bins_uploaded": list(raw_bins),
+               "calls_ms": [round(1e3 * x, 3) for x in times],
                "streamed": bool(_focuser.last_call.get("streamed")),
                "what": "pinned host inputs; the call copies the DEM, masks, trajectory and the "
                        "range bins the apertures can reach (device-computed bound) in pulse "

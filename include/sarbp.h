@@ -74,9 +74,9 @@ typedef struct sarbp_scene {
  * Tuning of the mixed-precision kernel.  An all-zero struct (or NULL) selects
  * the library default; sarbp_default_tuning() fills the defaults explicitly.
  * Supported: staged=0 with chunk 32/64 and tiles 32x8, 64x4, 16x16; staged=1,
- * 2 or 3 with chunk 32, 64 or 128 and (tile, window, stage) 16x16/160/32,
- * 16x16/160/16, 16x16/128/32, 16x8/128/32, 16x8/128/16, 32x8/128/32,
- * 64x4/128/32.  The staged kernels copy raw data in 16- or 32-pulse stages
+ * 2 or 3 with chunk 32, 64 or 128 and (tile, window, stage) 16x16/208/32,
+ * 16x16/192/32, 16x16/160/32, 16x16/160/16, 16x16/128/32, 16x8/128/32,
+ * 16x8/128/16, 32x8/128/32, 64x4/128/32.  The staged kernels copy raw data in 16- or 32-pulse stages
  * through a ring of 64 pulses; the chunk is the pulse group that shares one
  * float-float reference (mid-chunk pulse).  staged=2 and 3 run the staged
  * kernel on a persistent grid that drains a queue of the scene's tiles

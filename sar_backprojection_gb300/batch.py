@@ -27,11 +27,11 @@ from .focuser import resolve_tuning
 from .scene import DeviceScene
 
 # (tile0, tile1, window, chunk) variants of the staged kernel the autotuner times
-STAGED_TILINGS = ((16, 16, 160, 64), (16, 16, 160, 128), (16, 16, 128, 64), (16, 8, 128, 64),
+STAGED_TILINGS = ((16, 16, 208, 64), (16, 16, 208, 128), (16, 16, 160, 128), (16, 8, 128, 64),
                   (16, 8, 128, 128), (32, 8, 128, 64))
 
 
-def staged_tuning(tile0: int = 16, tile1: int = 16, window: int = 160, chunk: int = 64,
+def staged_tuning(tile0: int = 16, tile1: int = 16, window: int = 208, chunk: int = 64,
                   stage: int = 32) -> _lib.Tuning:
     return resolve_tuning({"chunk": chunk, "tile0": tile0, "tile1": tile1, "staged": 1,
                            "window": window, "stage": stage})

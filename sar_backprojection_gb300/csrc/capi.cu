@@ -108,11 +108,15 @@ bool build_params(const sarbp_scene *s, SceneParams *p)
 
 // Library default: the TMA-staged kernel with one CTA per tile, 64-pulse
 // chunks (one float-float reference per 64 pulses), 32-pulse stages, 16 x 16
-// pixel tiles with a 160-bin window.  On the 4000 x 250 / 40001-pulse
-// workload 128-pulse chunks measure 2 % faster, but halve the pulse spacing
-// at which the FP32 series gives way to the FP64 body; the cost-ordered tile
-// queue (staged=2) measured slower, its order scattering neighbouring tiles
-// in time and so losing the L2 reuse of their shared raw windows.
+// pixel tiles with a 208-bin window (two 53 KB stage buffers, still two CTAs
+// per SM).  A tile whose range spread at a stage exceeds the window runs that
+// stage on the scalar path with L2 reads; over rough terrain a 160-bin window
+// left 2.6 % of the 4000 x 250 / 40001-pulse workload's tiles 4-7x slower
+// and the whole launch 6 % slower.  On that workload 128-pulse chunks
+// measure 3 % faster, but halve the pulse spacing at which the FP32 series
+// gives way to the FP64 body; the cost-ordered tile queue (staged=2)
+// measured slower, its order scattering neighbouring tiles in time and so
+// losing the L2 reuse of their shared raw windows.
 bool valid_tuning(sarbp_tuning *t)
 {
     if (t->chunk == 0 && t->tile0 == 0 && t->tile1 == 0 && t->staged == 0) {
@@ -120,14 +124,14 @@ bool valid_tuning(sarbp_tuning *t)
         t->tile0 = 16;
         t->tile1 = 16;
         t->staged = 1;
-        t->window = 160;
+        t->window = 208;
     }
     if (t->chunk == 0) t->chunk = 32;
     if (t->tile0 == 0 && t->tile1 == 0) {
         t->tile0 = 16;
         t->tile1 = 16;
     }
-    if (t->staged && t->window == 0) t->window = (t->tile0 * t->tile1 >= 256) ? 160 : 128;
+    if (t->staged && t->window == 0) t->window = (t->tile0 * t->tile1 >= 256) ? 208 : 128;
     if (t->stage == 0) t->stage = 32;
     if (t->wait_polls < 0) {
         set_error("tuning.wait_polls must be >= 0 (got %d)", t->wait_polls);

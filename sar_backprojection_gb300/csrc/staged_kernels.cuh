@@ -978,8 +978,8 @@ int launch_batch_t(char *bws, const BatchLayout &BL, int64_t n_items, bool diag,
 // instantiated in staged_c32.cu / staged_c64.cu / staged_c128.cu.
 // SARBP_EINVAL (with a message) for a variant that is not built.
 #define SARBP_STAGED_TILES(X, C)                                                            \
-    X(C, 16, 16, 160, 32, 2) X(C, 16, 16, 160, 16, 4) X(C, 16, 16, 144, 32, 3)              \
-    X(C, 16, 16, 136, 32, 3) X(C, 16, 16, 128, 32, 2) X(C, 16, 8, 128, 32, 2)               \
+    X(C, 16, 16, 160, 32, 2) X(C, 16, 16, 160, 16, 4) X(C, 16, 16, 192, 32, 2)              \
+    X(C, 16, 16, 208, 32, 2) X(C, 16, 16, 128, 32, 2) X(C, 16, 8, 128, 32, 2)               \
     X(C, 16, 8, 128, 16, 4) X(C, 32, 8, 128, 32, 2) X(C, 64, 4, 128, 32, 2)
 
 template <int C>

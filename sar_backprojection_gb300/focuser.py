@@ -233,7 +233,10 @@ def _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache: _DropIn):
     out = res_cache.out_buffer(scene.npix, dev)
     lo, hi = scene.bin_lo, scene.bin_hi
     naz = scene.naz
-    marks = [naz * (k + 1) // blocks for k in range(blocks)]
+    # equal pulse blocks, the last one split in two: the tiles that end in
+    # the final block are the only work left after the copies, so it is small
+    marks = [naz * (k + 1) // blocks for k in range(blocks - 1)]
+    marks += [naz - naz // (2 * blocks), naz]
     ends = np.searchsorted(keys, np.asarray(marks, dtype=np.int64), side="right")
     ends[-1] = nt
     copy = res_cache.copy
@@ -247,7 +250,7 @@ def _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache: _DropIn):
     row = scene.pitch * 8
     first = 0
     a0 = 0
-    for k in range(blocks):
+    for k in range(len(marks)):
         a1 = marks[k]
         if hi >= lo and a1 > a0:
             _lib.check(lib.sarbp_upload_raw_bins(

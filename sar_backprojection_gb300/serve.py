@@ -22,6 +22,7 @@ is bit-identical whether it ran alone or in the mix.
 from __future__ import annotations
 
 import ctypes as C
+import gc
 import time
 from collections import deque
 from dataclasses import dataclass, field
@@ -213,6 +214,19 @@ class ServingEngine:
 
     def run(self, jobs: list[Job], clock=time.perf_counter, idle_sleep: float = 5e-5,
             timeout_s: float = 600.0) -> ServingReport:
+        # the loop runs with the cyclic garbage collector paused: its objects
+        # are freed by reference counting, and a full collection of a large
+        # interpreter heap stalls the loop (and every job in flight) for tens
+        # of milliseconds
+        gc_was_enabled = gc.isenabled()
+        gc.disable()
+        try:
+            return self._run(jobs, clock, idle_sleep, timeout_s)
+        finally:
+            if gc_was_enabled:
+                gc.enable()
+
+    def _run(self, jobs, clock, idle_sleep, timeout_s) -> ServingReport:
         arrivals = sorted(jobs, key=lambda j: j.arrival)
         pending: deque = deque()
         active: list[_Active] = []

@@ -30,7 +30,7 @@ TUNINGS = ([dict(chunk=c, tile0=t0, tile1=t1, staged=0) for c in (32, 64)
            + [dict(chunk=c, tile0=t0, tile1=t1, staged=s, window=w)
               for (c, s) in ((32, 1), (32, 2), (64, 1), (64, 2), (128, 1))
               for (t0, t1, w) in ((32, 8, 128), (64, 4, 128), (16, 16, 128), (16, 16, 160),
-                                  (16, 8, 128))]
+                                  (16, 16, 208), (16, 8, 128))]
            + [dict(chunk=c, tile0=t0, tile1=t1, staged=1, window=w, stage=16)
               for c in (32, 128) for (t0, t1, w) in ((16, 16, 160), (16, 8, 128))])
 TUNING_IDS = [f"c{t['chunk']}_{t['tile0']}x{t['tile1']}_"
@@ -159,6 +159,9 @@ def test_full_workload_fp64(full_scene, full_oracle):
                                     dict(chunk=64, tile0=16, tile1=16, staged=1, window=128),
                                     dict(chunk=64, tile0=32, tile1=8, staged=2, window=128),
                                     dict(chunk=128, tile0=16, tile1=16, staged=1, window=160),
+                                    dict(chunk=128, tile0=16, tile1=16, staged=1, window=208),
+                                    dict(chunk=128, tile0=16, tile1=16, staged=1, window=192),
+                                    dict(chunk=128, tile0=16, tile1=16, staged=3, window=208),
                                     dict(chunk=128, tile0=16, tile1=16, staged=1, window=160,
                                          stage=16),
                                     dict(chunk=64, tile0=16, tile1=8, staged=2, window=128,
@@ -166,7 +169,8 @@ def test_full_workload_fp64(full_scene, full_oracle):
                          ids=["c64_l1", "tma_16x16w128", "tma_16x16w160", "tma_16x8w128",
                               "tma_64x4w128", "queue_16x16w160", "queue_16x8w128",
                               "c64_tma_16x16w160", "c64_tma_16x16w128", "c64_queue_32x8w128",
-                              "c128_tma_16x16w160", "c128_tma_16x16w160s16",
+                              "c128_tma_16x16w160", "c128_tma_16x16w208", "c128_tma_16x16w192",
+                              "c128_byend_16x16w208", "c128_tma_16x16w160s16",
                               "c64_queue_16x8w128s16"])
 def test_full_workload_mixed(full_scene, full_oracle, tuning):
     """Mixed kernel variants against the full oracle image."""
