@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tuning", type=str, default="",
@@ -559,7 +559,7 @@ def run_ours(args, dist: Dist):
                 host["wgsx"], host["wgsy"], host["wgsz"], host["RawData"],
                 float(scene["NearRange"]), float(scene["DeltaRange"]), float(scene["Lambda"]),
                 host["Sint"])
-        for _ in range(5):
+        for _ in range(10):             # warm-up calls (host allocators, caches)
             FocalizzatoreBpPx(*argv, precision="mixed", tuning=tuning, device=dev)
         torch.cuda.synchronize(dev)
         dist.barrier()

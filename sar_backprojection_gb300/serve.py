@@ -3,17 +3,23 @@
 Requests (focusing jobs of different sizes) arrive over time.  The engine
 
 * admits a waiting job as soon as a scene slot and enough of the HBM budget
-  are free, uploading its inputs on a copy stream while other jobs' work runs
-  -- of host raw data only the range bins the job's apertures can reach
-  (the job's raw data and trajectory then stay resident until it finishes);
+  are free (at most ``ADMIT_PER_PASS`` per pass of the loop, so waves keep
+  launching during a burst of arrivals): its small inputs, chunk tables and
+  reachable-range-bin bound go through a setup stream of their own, so the
+  bound's read-back waits for this job's small copies only, and of host raw
+  data only the range bins its apertures can reach are then copied on the
+  copy stream (the job's raw data and trajectory stay resident until it
+  finishes);
 * runs the device in *waves*: each wave is one launch of the persistent
-  batch kernel whose work queue holds pixel tiles of every admitted job, so a
-  job that arrives while others are on the GPU joins the next wave and its
-  tiles run alongside theirs; waves alternate between two streams and two
-  batch workspaces, so the next wave is already on the device and its CTAs
-  fill the tail of the running one;
-* reads a job's image back (pinned host memory) when its last tile is done,
-  then frees its slot and memory.
+  batch kernel whose work queue holds pixel tiles of every resident job (one
+  whose raw copy the host has seen complete), so a job that arrives while
+  others are on the GPU joins a later wave and its tiles run alongside
+  theirs, and no wave ever waits for an upload; waves alternate between two
+  streams and two batch workspaces, so the next wave is already on the
+  device and its CTAs fill the tail of the running one;
+* reads a job's image back (pinned host memory, on a read-back stream that
+  no upload queues ahead of) when its last tile is done, then frees its slot
+  and memory.
 
 Latency = completion of the image's device-to-host copy minus arrival time.
 Per-tile work is the same code as the single-scene kernel, so a job's image
@@ -36,6 +42,7 @@ from .focuser import resolve_tuning
 from .scene import DeviceScene, scene_to_device
 
 GB = 1 << 30
+ADMIT_PER_PASS = 2     # admissions per pass of the serving loop
 
 
 def job_bytes(dim0: int, dim1: int, nra: int, naz: int) -> int:
@@ -78,7 +85,10 @@ class _Active:
     ws: torch.Tensor
     out: torch.Tensor
     host: torch.Tensor
-    tiles: deque                          # tile indices not yet launched, in cost order
+    ntiles: int                           # tiles of the job's scene
+    next_tile: int = 0                    # tiles [next_tile, ntiles) not yet launched
+    uploaded: torch.cuda.Event | None = None   # raw data and scene slot on the device
+    resident: bool = False                # the host has seen `uploaded` complete
     in_flight: int = 0
     done_event: torch.cuda.Event | None = None
 
@@ -121,7 +131,9 @@ class ServingEngine:
             raise ValueError("policy must be 'fifo' or 'srpt'")
         self.policy = policy
         self.compute = [torch.cuda.Stream(self.device), torch.cuda.Stream(self.device)]
-        self.copy = torch.cuda.Stream(self.device)
+        self.setup = torch.cuda.Stream(self.device)      # small inputs, tables, bound
+        self.copy = torch.cuda.Stream(self.device)       # raw range bins
+        self.readback = torch.cuda.Stream(self.device)   # images to host memory
         nb = _lib.check(int(self.lib.sarbp_batch_workspace_size(self.max_slots,
                                                                 self.wave_items)))
         self.bws_bytes = nb
@@ -135,16 +147,17 @@ class ServingEngine:
     def _admit(self, job: Job, now: float) -> _Active:
         slot = self.free_slots.pop(0)
         tb = C.byref(self.tuning)
-        with torch.cuda.stream(self.copy):
-            # host raw data in the reference's layout: only the range bins the
-            # job's apertures can reach go up (the bound is computed on the
-            # copy stream, which is all the admission synchronises)
-            scene = scene_to_device(*job.args, device=self.device, raw_bins="reached",
+        with torch.cuda.stream(self.setup):
+            # small inputs, chunk tables (prepared with the serving tuning) and
+            # the bound of the reachable range bins; the bound's read-back is
+            # the only synchronisation of an admission, and the setup stream
+            # holds no other job's raw copies
+            scene = scene_to_device(*job.args, device=self.device, raw_bins="bound",
                                     tuning=self.tuning)
             ws_bytes = _lib.check(int(self.lib.sarbp_mixed_workspace_size(
                 C.byref(scene.struct()), tb)))
             out = torch.empty((scene.npix, 2), dtype=torch.float64, device=self.device)
-            sp = self.copy.cuda_stream
+            sp = self.setup.cuda_stream
             if scene.workspace is not None and scene.workspace.numel() >= ws_bytes:
                 ws = scene.workspace            # prepared with this tuning on the way
             else:
@@ -156,17 +169,25 @@ class ServingEngine:
                 _lib.check(self.lib.sarbp_batch_set_scene(
                     b.data_ptr(), self.bws_bytes, self.max_slots, slot, C.byref(scene.struct()),
                     tb, ws.data_ptr(), ws_bytes, out.data_ptr(), None, None, sp))
-        ready = torch.cuda.Event()
-        ready.record(self.copy)
-        for st in self.compute:
-            st.wait_event(ready)
+        staged = torch.cuda.Event()
+        staged.record(self.setup)
+        # host raw data in the reference's layout: only the reachable range
+        # bins go up, queued behind the raw copies of earlier jobs
+        self.copy.wait_event(staged)
+        if scene.host_rows is not None and scene.bin_hi >= scene.bin_lo:
+            lo, n = scene.bin_lo, scene.bin_hi - scene.bin_lo + 1
+            _lib.check(self.lib.sarbp_upload_raw_bins(
+                scene.raw.data_ptr(), scene.pitch, scene.host_rows.data_ptr(), scene.nra,
+                lo, n, scene.naz, self.copy.cuda_stream))
+            scene.h2d_bytes += n * scene.naz * 8
+        uploaded = torch.cuda.Event()
+        uploaded.record(self.copy)
         job.admitted = now
-        job.nominal = _nominal(job.args)
         host = torch.empty((scene.npix, 2), dtype=torch.float64, pin_memory=True)
         self.used += job.nbytes()
         self.peak = max(self.peak, self.used)
         return _Active(job=job, slot=slot, scene=scene, ws=ws, out=out, host=host,
-                       tiles=deque(range(nt)))
+                       ntiles=nt, uploaded=uploaded)
 
     def _retire(self, a: _Active, now: float):
         j = a.job
@@ -178,23 +199,34 @@ class ServingEngine:
 
     # -- waves -------------------------------------------------------------
 
-    def _build_wave(self, active: list[_Active]) -> list[tuple[_Active, int]]:
-        cand = [a for a in active if a.tiles]
+    def _build_wave(self, active: list[_Active]) -> list[tuple[_Active, int, int]]:
+        """Up to ``wave_items`` tiles as (job, first, end) tile ranges, one per
+        job: FIFO takes the oldest jobs' tiles first, SRPT the jobs with the
+        fewest tiles left."""
+        cand = [a for a in active if a.next_tile < a.ntiles]
         if self.policy == "srpt":
-            cand.sort(key=lambda a: len(a.tiles))
+            cand.sort(key=lambda a: a.ntiles - a.next_tile)
         else:
             cand.sort(key=lambda a: a.job.arrival)
         wave = []
+        room = self.wave_items
         for a in cand:
-            while a.tiles and len(wave) < self.wave_items:
-                wave.append((a, a.tiles.popleft()))
-            if len(wave) >= self.wave_items:
+            if room == 0:
                 break
+            take = min(room, a.ntiles - a.next_tile)
+            wave.append((a, a.next_tile, a.next_tile + take))
+            a.next_tile += take
+            room -= take
         return wave
 
     def _launch_wave(self, wave, turn: int) -> torch.cuda.Event:
-        items = np.array([[a.slot, t] for a, t in wave], dtype=np.int32)
-        for a, _ in wave:
+        n = sum(t1 - t0 for _, t0, t1 in wave)
+        items = np.empty((n, 2), dtype=np.int32)        # (slot, tile) work items
+        k = 0
+        for a, t0, t1 in wave:
+            items[k:k + t1 - t0, 0] = a.slot
+            items[k:k + t1 - t0, 1] = np.arange(t0, t1, dtype=np.int32)
+            k += t1 - t0
             a.in_flight += 1
         stream, bws = self.compute[turn], self.bws[turn]
         with torch.cuda.stream(stream):
@@ -202,10 +234,10 @@ class ServingEngine:
             _lib.check(self.lib.sarbp_batch_set_items(bws.data_ptr(), self.bws_bytes,
                                                       self.max_slots,
                                                       items.ctypes.data_as(C.c_void_p),
-                                                      len(wave), sp))
+                                                      n, sp))
             _lib.check(self.lib.sarbp_batch_focus(bws.data_ptr(), self.bws_bytes,
                                                   self.max_slots, C.byref(self.tuning),
-                                                  len(wave), 0, None, sp))
+                                                  n, 0, None, sp))
         ev = torch.cuda.Event()
         ev.record(stream)
         return ev
@@ -244,10 +276,20 @@ class ServingEngine:
             while nxt < len(arrivals) and arrivals[nxt].arrival <= now:
                 pending.append(arrivals[nxt])
                 nxt += 1
-            # admission: FIFO, by slots and HBM budget
-            while pending and self.free_slots and self.used + pending[0].nbytes() <= self.budget:
+            progress = False
+            # admission: FIFO, by slots and HBM budget, a few per pass
+            admitted = 0
+            while (pending and admitted < ADMIT_PER_PASS and self.free_slots
+                   and self.used + pending[0].nbytes() <= self.budget):
                 active.append(self._admit(pending.popleft(), now))
-                launches += 1            # chunk tables (uploads are copies)
+                admitted += 1
+                launches += 3            # chunk tables, bound (2); uploads are copies
+                progress = True
+            # jobs whose raw copy has landed may join waves
+            for a in active:
+                if not a.resident and a.uploaded.query():
+                    a.resident = True
+                    progress = True
             if pending and not active and not self.free_slots:
                 raise RuntimeError("no scene slot free and nothing running")
             if pending and not active and self.used + pending[0].nbytes() > self.budget:
@@ -255,20 +297,20 @@ class ServingEngine:
             # completed waves
             while waves_in_flight and waves_in_flight[0][0].query():
                 _, wave, _ = waves_in_flight.popleft()
-                for a, _t in wave:
+                progress = True
+                for a, _t0, _t1 in wave:          # each job once per wave
                     a.in_flight -= 1
-                for a in {id(a): a for a, _ in wave}.values():
-                    if not a.tiles and a.in_flight == 0 and a.done_event is None:
+                    if a.next_tile >= a.ntiles and a.in_flight == 0 and a.done_event is None:
                         # every wave with this job's tiles has completed: read back
-                        with torch.cuda.stream(self.copy):
+                        with torch.cuda.stream(self.readback):
                             a.host.copy_(a.out, non_blocking=True)
                             ev = torch.cuda.Event()
-                            ev.record(self.copy)
+                            ev.record(self.readback)
                         a.done_event = ev
                         readbacks.append(a)
             # keep two waves queued on the device
             while len(waves_in_flight) < 2:
-                wave = self._build_wave(active)
+                wave = self._build_wave([a for a in active if a.resident])
                 if not wave:
                     break
                 turn = ws_turn
@@ -277,21 +319,27 @@ class ServingEngine:
                 waves_in_flight.append((ev, wave, turn))
                 nwaves += 1
                 launches += 1
+                progress = True
             # finished read-backs
             still = []
             for a in readbacks:
                 if a.done_event.query():
                     self._retire(a, clock() - t0)
                     active.remove(a)
+                    progress = True
                 else:
                     still.append(a)
             readbacks = still
             if nxt >= len(arrivals) and not pending and not active:
                 break
-            if idle_sleep:
+            if idle_sleep and not progress:
                 time.sleep(idle_sleep)
         torch.cuda.synchronize(self.device)
-        return ServingReport(jobs=jobs, wall_s=clock() - t0, waves=nwaves,
+        wall = clock() - t0
+        for j in jobs:                   # accounting, outside the timed loop
+            if not j.nominal:
+                j.nominal = _nominal(j.args)
+        return ServingReport(jobs=jobs, wall_s=wall, waves=nwaves,
                              gpu_launches=launches, peak_bytes=self.peak)
 
 

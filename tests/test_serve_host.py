@@ -1,5 +1,4 @@
 """Host logic of the serving engine (no GPU): arrivals, sizing, wave policy."""
-from collections import deque
 from types import SimpleNamespace
 
 import numpy as np
@@ -29,23 +28,23 @@ def _fake_engine(policy, wave_items):
 
 
 def _active(arrival, ntiles):
-    return SimpleNamespace(job=SimpleNamespace(arrival=arrival), tiles=deque(range(ntiles)))
+    return SimpleNamespace(job=SimpleNamespace(arrival=arrival), ntiles=ntiles, next_tile=0)
 
 
 def test_wave_fifo_fills_from_oldest_job():
     eng = _fake_engine("fifo", 5)
     a, b = _active(1.0, 3), _active(0.5, 4)
     wave = eng._build_wave([a, b])
-    assert [x is b for x, _ in wave] == [True] * 4 + [False]
-    assert len(b.tiles) == 0 and len(a.tiles) == 2
+    assert [(x is b, t0, t1) for x, t0, t1 in wave] == [(True, 0, 4), (False, 0, 1)]
+    assert b.next_tile == 4 and a.next_tile == 1
+    assert eng._build_wave([a, b]) == [(a, 1, 3)]
 
 
 def test_wave_srpt_prefers_short_jobs():
     eng = _fake_engine("srpt", 4)
     a, b = _active(0.0, 10), _active(5.0, 2)
     wave = eng._build_wave([a, b])
-    assert [x is b for x, _ in wave][:2] == [True, True]
-    assert len(wave) == 4
+    assert [(x is b, t0, t1) for x, t0, t1 in wave] == [(True, 0, 2), (False, 0, 2)]
 
 
 def test_summary_percentiles():
