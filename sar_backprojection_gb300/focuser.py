@@ -16,6 +16,7 @@ checkpoint has nothing to resume (long scenes use ``large_scene``).
 from __future__ import annotations
 
 import ctypes as C
+import sys
 from dataclasses import dataclass
 
 import numpy as np
@@ -151,13 +152,54 @@ def FocalizzatoreBpPx(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
 
 
 STREAM_BLOCKS = 8      # pulse blocks of a streamed drop-in upload
+IMAGE_POOL = 4         # host images the drop-in call keeps for reuse
+
+
+def _refs(a) -> int:
+    return sys.getrefcount(a)
+
+
+# references to an array held only by a list, counted as host_image counts them
+_POOL_ONLY_REFS = (lambda pool: _refs(pool[0]))([np.empty(1)])
+
+
+class HostImagePool:
+    """The complex128 (dim0, dim1) column-major host arrays the drop-in call
+    returns.
+
+    An array of an earlier call that the caller no longer references (no
+    variable, view or tensor holds it: only this pool does) is reused, its
+    pages already mapped; otherwise a new one is made.  A fresh 16 MB result
+    costs thousands of page faults inside the call, and a caller that keeps
+    the previous result while making the next call would pay them on every
+    call.  The pool keeps at most IMAGE_POOL arrays; beyond that the oldest is
+    left to the caller alone.
+    """
+
+    def __init__(self):
+        self.arrays: list[np.ndarray] = []
+
+    def get(self, dim0: int, dim1: int) -> np.ndarray:
+        for k in range(len(self.arrays)):
+            if (self.arrays[k].shape == (dim0, dim1)
+                    and _refs(self.arrays[k]) <= _POOL_ONLY_REFS):
+                return self.arrays[k]
+        a = np.empty((dim0, dim1), dtype=np.complex128, order="F")
+        self.arrays.append(a)
+        if len(self.arrays) > IMAGE_POOL:
+            self.arrays.pop(0)
+        return a
+
+    def clear(self) -> None:
+        self.arrays.clear()
 
 
 class _DropIn:
     """Per-device resources the synchronous drop-in call reuses across calls:
-    its copy and second compute stream and device buffers for the raw rows
-    and the image (a caller's repeated calls then allocate nothing on the
-    device).  The lock serialises calls from several host threads."""
+    its copy and second compute stream, device buffers for the raw rows and
+    the image (a caller's repeated calls then allocate nothing on the device)
+    and the pool of returned host images.  The lock serialises calls from
+    several host threads."""
 
     def __init__(self, dev: torch.device):
         import threading
@@ -166,6 +208,7 @@ class _DropIn:
         self.side = torch.cuda.Stream(dev)
         self.raw: dict[tuple, torch.Tensor] = {}
         self.out: dict[int, torch.Tensor] = {}
+        self.images = HostImagePool()
 
     def raw_buffer(self, nra: int, naz: int, dev) -> torch.Tensor:
         key = (naz, nra + (nra & 1))
@@ -190,6 +233,7 @@ def release_drop_in_buffers() -> None:
         with r.lock:
             r.raw.clear()
             r.out.clear()
+            r.images.clear()
 
 
 def _dropin_for(dev: torch.device) -> _DropIn:
@@ -271,7 +315,11 @@ def _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache: _DropIn):
         a0 = a1
     compute.wait_stream(side)
     res = FocusResult(image=out, workspace=ws)
-    img = res.to_numpy(scene.dim0, scene.dim1)
+    img = res_cache.images.get(scene.dim0, scene.dim1)
+    # column-major pixels: the F-order array's memory is the device image's
+    dst = torch.from_numpy(img.reshape(-1, order="F").view(np.float64)).view(-1, 2)
+    dst.copy_(out)
+    del dst
     res.check()
     return img, scene
 

@@ -60,3 +60,27 @@ def test_flatten_matches_numpy_fortran_order():
     m = np.array([[257, 1], [2, -255]])
     assert np.array_equal(flatten_f(m, np.uint8, "cpu").numpy(),
                           m.astype(np.uint8).flatten(order="F"))
+
+
+def test_host_image_pool_reuses_only_unreferenced_arrays():
+    """The drop-in call's result arrays are reused only once nothing of the
+    caller's refers to them: a held array, a view of it or a tensor over it
+    keeps it out of reach of later calls."""
+    from sar_backprojection_gb300.focuser import IMAGE_POOL, HostImagePool
+    pool = HostImagePool()
+    a = pool.get(4, 3)
+    assert a.shape == (4, 3) and a.dtype == np.complex128 and a.flags.f_contiguous
+    b = pool.get(4, 3)
+    assert b is not a                              # a is held by the caller
+    del a
+    c = pool.get(4, 3)
+    assert c is pool.arrays[0]                     # dropped: reused
+    view = c[1:]
+    t = torch.from_numpy(b.reshape(-1, order="F").view(np.float64))
+    d = pool.get(4, 3)
+    assert d is not c and d is not b
+    del view, t
+    assert pool.get(5, 3).shape == (5, 3)           # another shape: a new array
+    held = [pool.get(2, 2) for _ in range(IMAGE_POOL + 2)]
+    assert len({id(x) for x in held}) == len(held)
+    assert len(pool.arrays) <= IMAGE_POOL

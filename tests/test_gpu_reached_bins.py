@@ -99,3 +99,11 @@ def test_streamed_drop_in_equals_resident_focus(name):
                                             window=128)).check().to_numpy(full.dim0, full.dim1)
     assert np.array_equal(np.ascontiguousarray(img1).view(np.uint64),
                           np.ascontiguousarray(ref1).view(np.uint64))
+    # the first result, held across the second call, was not reused for it
+    assert img1 is not img
+    assert np.array_equal(np.ascontiguousarray(img).view(np.uint64),
+                          np.ascontiguousarray(ref).view(np.uint64))
+    del img1
+    img2 = FocalizzatoreBpPx(*args, precision="mixed")
+    assert np.array_equal(np.ascontiguousarray(img2).view(np.uint64),
+                          np.ascontiguousarray(ref).view(np.uint64))
