@@ -6,7 +6,9 @@
 // round-half-to-even range bins, bins kept iff 0 <= bin < Nra-1, pulses kept
 // iff 0 < a < Naz-1.  Every geometry operation is an explicitly rounded IEEE
 // op (no FMA contraction) so that range bins are bit-identical to the FP64
-// CPU result; cos/sin are CUDA's double-precision functions.
+// CPU result; the division by DeltaRange is a product with its reciprocal
+// except within a tie band where only the correctly rounded quotient decides
+// the bin (exact_bin_recip); cos/sin are CUDA's double-precision functions.
 //
 // Raw data are read where they lie in HBM, in the reference's column-major
 // (Nra, Naz) complex64 layout: no host-side transpose into split planes.
@@ -31,11 +33,12 @@ focus_fp64_kernel(const SceneParams P, double2 *__restrict__ out,
     int64_t lo, hi;
     if (pixel_aperture(P.mask[ii], P.sint[ii], P.index[ii], P.naz, &lo, &hi)) {
         const double px = P.x[ii], py = P.y[ii], pz = P.z[ii];
+        const double inv_dra = __ddiv_rn(1.0, P.dra);
         for (int64_t a = lo; a <= hi; ++a) {
             double r2, r;
-            const int64_t bin = exact_bin(px, py, pz, __ldg(P.tx + a), __ldg(P.ty + a),
-                                          __ldg(P.tz + a), P.near_range, P.dra, P.nra,
-                                          &r2, &r);
+            const int64_t bin = exact_bin_recip(px, py, pz, __ldg(P.tx + a), __ldg(P.ty + a),
+                                                __ldg(P.tz + a), P.near_range, P.dra, inv_dra,
+                                                P.nra, &r2, &r);
             if (bin < 0) continue;
             // phase = ((-4*pi)/lambda)*R + beta*R^2 ; filter = exp(-j*phase)
             const double phase = __dadd_rn(__dmul_rn(P.k4pl, r), __dmul_rn(P.beta, r2));

@@ -95,6 +95,37 @@ __device__ inline int64_t exact_bin(double px, double py, double pz,
     return (int64_t)fb;
 }
 
+// exact_bin with the division by dra replaced by a product with inv_dra =
+// RN(1/dra), except near a .5 tie.  With q = (R - near)/dra exactly,
+// f = RN((R - near) * inv_dra) is within |q| * 2^-52 of q and the reference's
+// RN(q) within |q| * 2^-53, so rint(f) equals the reference's rint(RN(q))
+// unless a half-integer lies within |f| * 2^-51 of f; in that band (and only
+// there) the correctly rounded quotient is formed.  Same bins, same r2 and r.
+__device__ inline int64_t exact_bin_recip(double px, double py, double pz,
+                                          double tx, double ty, double tz,
+                                          double near_range, double dra, double inv_dra,
+                                          int64_t nra, double *r2_out, double *r_out)
+{
+    const double xc = __dsub_rn(px, tx);
+    const double yc = __dsub_rn(py, ty);
+    const double zc = __dsub_rn(pz, tz);
+    const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(xc, xc), __dmul_rn(yc, yc)),
+                                __dmul_rn(zc, zc));
+    const double r = __dsqrt_rn(r2);
+    const double num = __dsub_rn(r, near_range);
+    double f = __dmul_rn(num, inv_dra);
+    double fb = rint(f);
+    // f - rint(f) is exact; 2^-51 |f| bounds |f - RN(q)| with margin
+    if (fabs(__dsub_rn(f, fb)) >= 0.5 - fabs(f) * 0x1p-51 - 0x1p-1000) {
+        f = __ddiv_rn(num, dra);
+        fb = rint(f);
+    }
+    *r2_out = r2;
+    *r_out = r;
+    if (!(fb < (double)(nra - 1) && fb >= 0.0)) return -1;
+    return (int64_t)fb;
+}
+
 // Device status block at the head of every workspace.
 struct StatusBlock {
     unsigned int error;      // non-zero: a bounded wait gave up
