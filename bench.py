@@ -12,8 +12,10 @@ Printed (rank 0, one JSON line):
             host inputs: H2D of every input, focusing, D2H of the image
   fp64      the plain FP64 kernel on the same scene (the comparator)
   quality   mixed image vs the FP64 kernel's image (which matches the oracle)
-  roofline  FP32/SFU issue roofline of the main kernel (probe-measured peaks),
-            roofline_hbm the same kernel against measured HBM bandwidth
+  roofline  the main kernel's algorithmic bytes per launch against the measured
+            HBM bandwidth, with ncu DRAM traffic; roofline_issue the same
+            kernel against its real bound, the FP32/SFU issue roofline
+            (probe-measured peaks); roofline_fp64 the FP64 kernel
   cpu_baseline  the oracle's C restatement on the host cores, bounded sample
 
 ``--impl reference`` times the reference algorithm's CPU implementation (the
@@ -51,7 +53,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--e2e-steps", type=int, default=200)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tuning", type=str, default="",
@@ -584,12 +586,18 @@ def run_ours(args, dist: Dist):
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "ms_per_step": 1e3 * e2e_s, "api": "FocalizzatoreBpPx(..., precision='mixed')",
                "raw_bins_uploaded": list(raw_bins),
+               "calls": len(times),
+               "p50_ms": 1e3 * float(np.percentile(times, 50)),
+               "p99_ms": 1e3 * float(np.percentile(times, 99)),
+               "max_ms": 1e3 * max(times),
+               "value_at_p50": dist.world * work / float(np.percentile(times, 50)) / 1e9,
                "calls_ms": [round(1e3 * x, 3) for x in times],
                "streamed": bool(_focuser.last_call.get("streamed")),
                "what": "pinned host inputs; the call copies the DEM, masks, trajectory and the "
                        "range bins the apertures can reach (device-computed bound) in pulse "
                        "blocks overlapped by focusing, and returns the complex128 image in "
-                       "host memory"}
+                       "host memory; value = work / mean call time over every timed call "
+                       "(no call dropped), value_at_p50 the same at the median call"}
         ts = sorted(times)
         lat = {"p50_ms": 1e3 * float(np.percentile(ts, 50)),
                "p99_ms": 1e3 * float(np.percentile(ts, 99)),
