@@ -225,6 +225,19 @@ SARBP_API int sarbp_raw_bin_range(const sarbp_scene *scene, const sarbp_tuning *
                                   void *stream);
 
 /*
+ * sarbp_raw_bin_range without the synchronisation: the bound is computed and
+ * copied into host_range[0..1] (int32, page-locked host memory for the copy
+ * to be asynchronous) in stream order, as [1, 0] when no pixel has an
+ * aperture; the values are valid once `stream` has passed this call (an
+ * event recorded after it has completed).  Lets a serving loop admit a job
+ * without waiting for the copies queued ahead of it.  No reference
+ * counterpart.
+ */
+SARBP_API int sarbp_raw_bin_range_async(const sarbp_scene *scene, const sarbp_tuning *tuning,
+                                        void *workspace, size_t workspace_bytes,
+                                        int32_t *host_range, void *stream);
+
+/*
  * Host -> device copy of range bins [bin_lo, bin_lo + nbins) of `npulses`
  * pulse rows (complex64, row pitches in elements) into the same positions of
  * a device raw buffer: one 2-D copy, asynchronous when `src` is pinned.

@@ -88,6 +88,8 @@ SIGNATURES = {
                                           _P, C.c_size_t, C.c_int64, C.c_int64, _P]),
     "sarbp_raw_bin_range": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, C.c_size_t,
                                       C.POINTER(C.c_int64), _P]),
+    "sarbp_raw_bin_range_async": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P,
+                                            C.c_size_t, _P, _P]),
     "sarbp_upload_raw_bins": (C.c_int, [_P, C.c_int64, _P, C.c_int64, C.c_int64, C.c_int64,
                                         C.c_int64, _P]),
     "sarbp_focus_mixed_noalloc": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, _P, _P,

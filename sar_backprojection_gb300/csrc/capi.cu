@@ -292,6 +292,18 @@ SARBP_API int sarbp_raw_bin_range(const sarbp_scene *scene, const sarbp_tuning *
                          static_cast<cudaStream_t>(stream));
 }
 
+SARBP_API int sarbp_raw_bin_range_async(const sarbp_scene *scene, const sarbp_tuning *tuning,
+                                        void *workspace, size_t workspace_bytes,
+                                        int32_t *host_range, void *stream)
+{
+    SceneParams P;
+    sarbp_tuning T;
+    int rc = mixed_args(scene, tuning, &P, &T);
+    if (rc) return rc;
+    return raw_bin_range_async(P, T, workspace, workspace_bytes, host_range,
+                               static_cast<cudaStream_t>(stream));
+}
+
 SARBP_API int sarbp_upload_raw_bins(void *dst, int64_t dst_pitch, const void *src,
                                     int64_t src_pitch, int64_t bin_lo, int64_t nbins,
                                     int64_t npulses, void *stream)

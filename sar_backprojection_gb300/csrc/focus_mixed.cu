@@ -443,17 +443,34 @@ __global__ void range_init_kernel(int *range)
     range[1] = INT_MIN;
 }
 
-int raw_bin_range(const SceneParams &P, const sarbp_tuning &T, void *workspace, size_t ws_bytes,
-                  int64_t *range, cudaStream_t stream)
+// The reduced interval as the entry points report it: [1, 0] when no pixel
+// has an aperture, else clamped to the bins 0..nra-1 of a pulse row.
+__global__ void range_finish_kernel(int *range, int64_t nra)
+{
+    const int lo = range[0], hi = range[1];
+    if (lo > hi) {
+        range[0] = 1;
+        range[1] = 0;
+    } else {
+        range[0] = lo < 0 ? 0 : lo;
+        range[1] = (int64_t)hi > nra - 1 ? (int)(nra - 1) : hi;
+    }
+}
+
+// Enqueue the bound of the reachable bins and its copy into host[0..1]
+// (int32), then clear the status block's spare words again (read by
+// sarbp_mixed_status).  Nothing is synchronised.
+static int raw_bin_range_enqueue(const SceneParams &P, const sarbp_tuning &T, void *workspace,
+                                 size_t ws_bytes, int32_t *host, const char *who,
+                                 cudaStream_t stream)
 {
     const MixedLayout L = mixed_layout(P, T);
-    if (!workspace || ws_bytes < L.total || !range) {
-        set_error("sarbp_raw_bin_range: workspace (%zu < %zu bytes) or range missing", ws_bytes,
-                  L.total);
+    if (!workspace || ws_bytes < L.total || !host) {
+        set_error("%s: workspace (%zu < %zu bytes) or range missing", who, ws_bytes, L.total);
         return SARBP_EWORKSPACE;
     }
     if (!T.staged) {
-        set_error("sarbp_raw_bin_range: needs tables prepared with a staged tuning");
+        set_error("%s: needs tables prepared with a staged tuning", who);
         return SARBP_EINVAL;
     }
     char *ws = static_cast<char *>(workspace);
@@ -479,25 +496,38 @@ int raw_bin_range(const SceneParams &P, const sarbp_tuning &T, void *workspace, 
         raw_bin_range_gmem_kernel<<<(unsigned)((P.npix + 255) / 256), 256, 0, stream>>>(
             P, pff, sdv, T.stage, dr);
     }
+    range_finish_kernel<<<1, 1, 0, stream>>>(dr, P.nra);
     rc = cuda_status(cudaGetLastError(), "raw_bin_range launch");
     if (rc) return rc;
-    int h[2];
-    rc = cuda_status(cudaMemcpyAsync(h, dr, sizeof(h), cudaMemcpyDeviceToHost, stream),
+    rc = cuda_status(cudaMemcpyAsync(host, dr, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                     stream),
                      "raw_bin_range read");
+    if (rc) return rc;
+    return cuda_status(cudaMemsetAsync(dr, 0, 2 * sizeof(int), stream), "raw_bin_range clear");
+}
+
+int raw_bin_range(const SceneParams &P, const sarbp_tuning &T, void *workspace, size_t ws_bytes,
+                  int64_t *range, cudaStream_t stream)
+{
+    if (!range) {
+        set_error("sarbp_raw_bin_range: range missing");
+        return SARBP_EINVAL;
+    }
+    int32_t h[2];
+    int rc = raw_bin_range_enqueue(P, T, workspace, ws_bytes, h, "sarbp_raw_bin_range", stream);
     if (rc) return rc;
     rc = cuda_status(cudaStreamSynchronize(stream), "raw_bin_range synchronize");
     if (rc) return rc;
-    // clear the spare words again (the status block is read by sarbp_mixed_status)
-    rc = cuda_status(cudaMemsetAsync(dr, 0, 2 * sizeof(int), stream), "raw_bin_range clear");
-    if (rc) return rc;
-    if (h[0] > h[1]) {
-        range[0] = 1;
-        range[1] = 0;
-        return SARBP_OK;
-    }
-    range[0] = h[0] < 0 ? 0 : h[0];
-    range[1] = (int64_t)h[1] > P.nra - 1 ? P.nra - 1 : h[1];
+    range[0] = h[0];
+    range[1] = h[1];
     return SARBP_OK;
+}
+
+int raw_bin_range_async(const SceneParams &P, const sarbp_tuning &T, void *workspace,
+                        size_t ws_bytes, int32_t *host_range, cudaStream_t stream)
+{
+    return raw_bin_range_enqueue(P, T, workspace, ws_bytes, host_range,
+                                 "sarbp_raw_bin_range_async", stream);
 }
 
 static int check_workspace(const MixedLayout &L, void *workspace, size_t ws_bytes)

@@ -99,6 +99,15 @@ static int tiling_tiles(const SceneParams &P, const sarbp_tuning &T, int64_t *nt
     return SARBP_OK;
 }
 
+// Stores one batch scene descriptor.  The descriptor travels as a kernel
+// parameter: the write is stream-ordered like a copy, but the host neither
+// waits for the stream (a copy from pageable host memory would) nor has to
+// keep a pinned copy alive until it executes.
+__global__ void store_batch_scene_kernel(BatchScene *dst, const __grid_constant__ BatchScene B)
+{
+    if (threadIdx.x == 0) *dst = B;
+}
+
 int batch_set_scene(void *bws, size_t bytes, int slot, int nscenes, const SceneParams &P,
                     const sarbp_tuning &T, void *scene_ws, size_t scene_ws_bytes, double *out,
                     int32_t *nvalid, uint64_t *checksum, cudaStream_t stream)
@@ -130,8 +139,8 @@ int batch_set_scene(void *bws, size_t bytes, int slot, int nscenes, const SceneP
     rc = tiling_tiles(P, T, &B.ntile0, &B.ntiles);
     if (rc) return rc;
     char *dst = static_cast<char *>(bws) + BL.scenes + sizeof(BatchScene) * (size_t)slot;
-    return cuda_status(cudaMemcpyAsync(dst, &B, sizeof(B), cudaMemcpyHostToDevice, stream),
-                       "batch scene upload");
+    store_batch_scene_kernel<<<1, 32, 0, stream>>>(reinterpret_cast<BatchScene *>(dst), B);
+    return cuda_status(cudaGetLastError(), "batch scene upload");
 }
 
 int batch_set_items(void *bws, size_t bytes, int nscenes, const int32_t *items, int64_t n,

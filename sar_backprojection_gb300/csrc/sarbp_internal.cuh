@@ -166,6 +166,8 @@ int launch_focus_fp64(const SceneParams &P, double *out, int32_t *nvalid, uint64
                       cudaStream_t stream);
 int raw_bin_range(const SceneParams &P, const sarbp_tuning &T, void *workspace, size_t ws_bytes,
                   int64_t *range, cudaStream_t stream);
+int raw_bin_range_async(const SceneParams &P, const sarbp_tuning &T, void *workspace,
+                        size_t ws_bytes, int32_t *host_range, cudaStream_t stream);
 int launch_mixed_range(const SceneParams &P, const sarbp_tuning &T, void *workspace,
                        size_t ws_bytes, int64_t first, int64_t count, double *out,
                        int32_t *nvalid, uint64_t *checksum, uint64_t *counters,

@@ -105,6 +105,8 @@ class DeviceScene:
     h2d_bytes: int = 0
     workspace: torch.Tensor | None = field(default=None, repr=False)
     host_rows: torch.Tensor | None = field(default=None, repr=False)
+    # raw_bins="deferred": pinned int32 pair the bound is copied into
+    bound_host: torch.Tensor | None = field(default=None, repr=False)
 
     @property
     def npix(self) -> int:
@@ -191,10 +193,43 @@ def _upload_reached_bins(scene: "DeviceScene", host_rows: torch.Tensor, upload: 
     scene.workspace = ws
 
 
+def _bound_reached_bins_async(scene: "DeviceScene", bound_host: torch.Tensor,
+                              tuning=None) -> None:
+    """Enqueue the chunk tables and the reachable-bin bound with its copy
+    into ``bound_host`` (pinned int32[2], sarbp_raw_bin_range_async) on the
+    current stream, without waiting for it; ``read_bound`` takes it once the
+    stream has passed."""
+    from .focuser import resolve_tuning
+    lib = _lib.load()
+    dev = scene.device
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    t = resolve_tuning(tuning)
+    sc = C.byref(scene.struct())
+    need = _lib.check(int(lib.sarbp_mixed_workspace_size(sc, C.byref(t))))
+    ws = torch.empty(need, dtype=torch.uint8, device=dev)
+    _lib.check(lib.sarbp_mixed_prepare(sc, C.byref(t), ws.data_ptr(), need, stream))
+    _lib.check(lib.sarbp_raw_bin_range_async(sc, C.byref(t), ws.data_ptr(), need,
+                                             bound_host.data_ptr(), stream))
+    scene.workspace = ws
+    scene.bound_host = bound_host
+
+
+def read_bound(scene: "DeviceScene") -> tuple[int, int]:
+    """The bound a raw_bins="deferred" upload enqueued, as (bin_lo, bin_hi)
+    (bin_lo > bin_hi: no bin is reached); call it once the stream the scene
+    was uploaded on has passed the bound (an event recorded after the upload
+    has completed)."""
+    if scene.bound_host is not None:
+        scene.bin_lo, scene.bin_hi = int(scene.bound_host[0]), int(scene.bound_host[1])
+        scene.bound_host = None
+    return scene.bin_lo, scene.bin_hi
+
+
 def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
                     near_range, dra, lambda_val, Sint, device=None,
                     raw_bins: str = "all", tuning=None,
-                    raw_buffer: torch.Tensor | None = None) -> DeviceScene:
+                    raw_buffer: torch.Tensor | None = None,
+                    bound_host: torch.Tensor | None = None) -> DeviceScene:
     """Upload the reference's 13 focusing arguments (same order) to the device.
 
     Raises ValueError where the reference does (Raw_Data or xxg1 not 2-D,
@@ -210,12 +245,18 @@ def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
     whole.  ``raw_bins="bound"``: the same bound, but no raw row is copied
     (the caller streams them; ``scene.host_rows`` is the host source) and
     ``scene.workspace`` holds tables prepared with ``tuning``.
+    ``raw_bins="deferred"``: as "bound", but the bound is not waited for: it
+    is copied into ``bound_host`` (pinned int32[2]) in stream order and
+    ``read_bound`` takes it later.
     ``raw_buffer``: a float32 (Naz, pitch, 2) device tensor to receive the
-    raw rows in those two modes instead of a new allocation (the caller owns
+    raw rows in those modes instead of a new allocation (the caller owns
     its reuse).
     """
-    if raw_bins not in ("all", "reached", "bound"):
-        raise ValueError(f"raw_bins must be 'all', 'reached' or 'bound', got {raw_bins!r}")
+    if raw_bins not in ("all", "reached", "bound", "deferred"):
+        raise ValueError("raw_bins must be 'all', 'reached', 'bound' or 'deferred', "
+                         f"got {raw_bins!r}")
+    if raw_bins == "deferred" and bound_host is None:
+        raise ValueError("raw_bins='deferred' needs a pinned int32[2] bound_host")
     raw_shape = tuple(Raw_Data.shape)
     if len(raw_shape) != 2:
         raise ValueError("Raw_Data must be a 2D array")
@@ -267,8 +308,11 @@ def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
                                                         scene.ty, scene.tz))
     if host_rows is not None:
         scene.h2d_bytes = small
-        _upload_reached_bins(scene, host_rows, upload=raw_bins == "reached", tuning=tuning)
-        scene.host_rows = host_rows if raw_bins == "bound" else None
+        if raw_bins == "deferred":
+            _bound_reached_bins_async(scene, bound_host, tuning=tuning)
+        else:
+            _upload_reached_bins(scene, host_rows, upload=raw_bins == "reached", tuning=tuning)
+        scene.host_rows = host_rows if raw_bins in ("bound", "deferred") else None
     else:
         scene.bin_lo, scene.bin_hi = 0, nra - 1
         scene.h2d_bytes = small + (nra * naz * 8 if Raw_Data is not None and

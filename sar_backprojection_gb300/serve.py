@@ -4,10 +4,11 @@ Requests (focusing jobs of different sizes) arrive over time.  The engine
 
 * admits a waiting job as soon as a scene slot and enough of the HBM budget
   are free (at most ``ADMIT_PER_PASS`` per pass of the loop, so waves keep
-  launching during a burst of arrivals): its small inputs, chunk tables and
-  reachable-range-bin bound go through a setup stream of their own, so the
-  bound's read-back waits for this job's small copies only, and of host raw
-  data only the range bins its apertures can reach are then copied on the
+  launching during a burst of arrivals), without waiting for the GPU: its
+  small inputs, chunk tables and reachable-range-bin bound are queued on a
+  setup stream of their own, the bound comes back to pinned host memory in
+  stream order, and on a later pass, once the host sees it, only the range
+  bins the job's apertures can reach are copied from host raw data on the
   copy stream (the job's raw data and trajectory stay resident until it
   finishes);
 * runs the device in *waves*: each wave is one launch of the persistent
@@ -39,7 +40,7 @@ import torch
 from . import _lib
 from .batch import staged_tuning
 from .focuser import resolve_tuning
-from .scene import DeviceScene, scene_to_device
+from .scene import DeviceScene, read_bound, scene_to_device
 
 GB = 1 << 30
 ADMIT_PER_PASS = 2     # admissions per pass of the serving loop
@@ -87,7 +88,8 @@ class _Active:
     host: torch.Tensor
     ntiles: int                           # tiles of the job's scene
     next_tile: int = 0                    # tiles [next_tile, ntiles) not yet launched
-    uploaded: torch.cuda.Event | None = None   # raw data and scene slot on the device
+    staged: torch.cuda.Event | None = None     # small inputs, tables, bound, scene slot
+    uploaded: torch.cuda.Event | None = None   # raw data on the device (copy issued)
     resident: bool = False                # the host has seen `uploaded` complete
     in_flight: int = 0
     done_event: torch.cuda.Event | None = None
@@ -139,6 +141,9 @@ class ServingEngine:
         self.bws_bytes = nb
         self.bws = [torch.empty(nb, dtype=torch.uint8, device=self.device) for _ in range(2)]
         self.free_slots = list(range(self.max_slots))
+        # per slot: the reachable-bin bound of the job in it (pinned, written
+        # by the device in stream order)
+        self.bounds = torch.empty((self.max_slots, 2), dtype=torch.int32, pin_memory=True)
         self.used = 0
         self.peak = 0
 
@@ -148,12 +153,12 @@ class ServingEngine:
         slot = self.free_slots.pop(0)
         tb = C.byref(self.tuning)
         with torch.cuda.stream(self.setup):
-            # small inputs, chunk tables (prepared with the serving tuning) and
-            # the bound of the reachable range bins; the bound's read-back is
-            # the only synchronisation of an admission, and the setup stream
-            # holds no other job's raw copies
-            scene = scene_to_device(*job.args, device=self.device, raw_bins="bound",
-                                    tuning=self.tuning)
+            # small inputs, chunk tables (prepared with the serving tuning),
+            # the reachable-bin bound into this slot's pinned pair and the
+            # batch scene slot, all queued on the setup stream: nothing here
+            # waits for the GPU
+            scene = scene_to_device(*job.args, device=self.device, raw_bins="deferred",
+                                    tuning=self.tuning, bound_host=self.bounds[slot])
             ws_bytes = _lib.check(int(self.lib.sarbp_mixed_workspace_size(
                 C.byref(scene.struct()), tb)))
             out = torch.empty((scene.npix, 2), dtype=torch.float64, device=self.device)
@@ -171,23 +176,28 @@ class ServingEngine:
                     tb, ws.data_ptr(), ws_bytes, out.data_ptr(), None, None, sp))
         staged = torch.cuda.Event()
         staged.record(self.setup)
-        # host raw data in the reference's layout: only the reachable range
-        # bins go up, queued behind the raw copies of earlier jobs
-        self.copy.wait_event(staged)
-        if scene.host_rows is not None and scene.bin_hi >= scene.bin_lo:
-            lo, n = scene.bin_lo, scene.bin_hi - scene.bin_lo + 1
-            _lib.check(self.lib.sarbp_upload_raw_bins(
-                scene.raw.data_ptr(), scene.pitch, scene.host_rows.data_ptr(), scene.nra,
-                lo, n, scene.naz, self.copy.cuda_stream))
-            scene.h2d_bytes += n * scene.naz * 8
-        uploaded = torch.cuda.Event()
-        uploaded.record(self.copy)
         job.admitted = now
         host = torch.empty((scene.npix, 2), dtype=torch.float64, pin_memory=True)
         self.used += job.nbytes()
         self.peak = max(self.peak, self.used)
         return _Active(job=job, slot=slot, scene=scene, ws=ws, out=out, host=host,
-                       ntiles=nt, uploaded=uploaded)
+                       ntiles=nt, staged=staged)
+
+    def _start_upload(self, a: _Active) -> None:
+        """The job's setup has completed: copy its reachable raw bins (host raw
+        data in the reference's layout), queued behind earlier jobs' copies."""
+        scene = a.scene
+        self.copy.wait_event(a.staged)
+        if scene.host_rows is not None:
+            lo, hi = read_bound(scene)
+            if hi >= lo:
+                n = hi - lo + 1
+                _lib.check(self.lib.sarbp_upload_raw_bins(
+                    scene.raw.data_ptr(), scene.pitch, scene.host_rows.data_ptr(), scene.nra,
+                    lo, n, scene.naz, self.copy.cuda_stream))
+                scene.h2d_bytes += n * scene.naz * 8
+        a.uploaded = torch.cuda.Event()
+        a.uploaded.record(self.copy)
 
     def _retire(self, a: _Active, now: float):
         j = a.job
@@ -283,11 +293,16 @@ class ServingEngine:
                    and self.used + pending[0].nbytes() <= self.budget):
                 active.append(self._admit(pending.popleft(), now))
                 admitted += 1
-                launches += 3            # chunk tables, bound (2); uploads are copies
+                launches += 4            # chunk tables, bound (3); uploads are copies
                 progress = True
-            # jobs whose raw copy has landed may join waves
+            # jobs whose setup has completed get their raw copy; jobs whose
+            # raw copy has landed may join waves
             for a in active:
-                if not a.resident and a.uploaded.query():
+                if a.uploaded is None:
+                    if a.staged.query():
+                        self._start_upload(a)
+                        progress = True
+                elif not a.resident and a.uploaded.query():
                     a.resident = True
                     progress = True
             if pending and not active and not self.free_slots:

@@ -137,6 +137,11 @@ def test_new_entry_points_reject_bad_arguments_without_a_gpu():
     # bound without a workspace
     assert lib.sarbp_raw_bin_range(C.byref(s), C.byref(t), None, 0, rng,
                                    None) == _lib.SARBP_EWORKSPACE
+    hr = (C.c_int32 * 2)()
+    assert lib.sarbp_raw_bin_range_async(C.byref(s), C.byref(t), None, 0, hr,
+                                         None) == _lib.SARBP_EWORKSPACE
+    assert lib.sarbp_raw_bin_range(C.byref(s), C.byref(t), C.c_void_p(0x4000), 1 << 30,
+                                   None, None) == _lib.SARBP_EINVAL
     # queue range / keys need a queued tuning
     out = C.c_void_p(0x3000)
     assert lib.sarbp_focus_mixed_range(C.byref(s), C.byref(t), out, None, None, None,
