@@ -379,14 +379,18 @@ def run_serving(args, dev):
 
 
 TUNING_FIELDS = ("chunk", "tile0", "tile1", "staged", "window", "stage")
-# staged-kernel variants timed on the workload itself; the fastest is measured
-AUTOTUNE_CANDIDATES = ((64, 16, 16, 1, 208, 32), (128, 16, 16, 1, 208, 32),
+# staged-kernel variants timed on the workload itself, in order of preference
+# (widest window first); the first within 1 % of the fastest is measured
+AUTOTUNE_CANDIDATES = ((128, 16, 16, 1, 208, 32), (64, 16, 16, 1, 208, 32),
                        (128, 16, 16, 1, 192, 32), (128, 16, 16, 1, 160, 32))
 
 
 def pick_tuning(lib, ds, dev, candidates=AUTOTUNE_CANDIDATES, reps: int = 5):
     """Time each candidate tuning on the resident scene (prepare + focus per
-    step, CUDA events) and return the fastest with all timings."""
+    step, CUDA events) and return, with all timings, the first candidate (in
+    the listed order of preference) within 1 % of the fastest: run-to-run
+    noise is about that, and the earlier candidates' wider windows leave no
+    stage to the slower path."""
     import ctypes as C
 
     import torch
@@ -397,7 +401,7 @@ def pick_tuning(lib, ds, dev, candidates=AUTOTUNE_CANDIDATES, reps: int = 5):
     sc = C.byref(ds.struct())
     out = torch.empty((ds.npix, 2), dtype=torch.float64, device=dev)
     sp = torch.cuda.current_stream(dev).cuda_stream
-    best, times = None, {}
+    timed, times = [], {}
     for cand in candidates:
         t = resolve_tuning(dict(zip(TUNING_FIELDS, cand)))
         tb = C.byref(t)
@@ -418,10 +422,10 @@ def pick_tuning(lib, ds, dev, candidates=AUTOTUNE_CANDIDATES, reps: int = 5):
         torch.cuda.synchronize(dev)
         ms = a.elapsed_time(b) / reps
         times[",".join(map(str, cand))] = round(ms, 4)
-        if best is None or ms < best[0]:
-            best = (ms, t)
+        timed.append((ms, t))
         del ws
-    return best[1], times
+    fastest = min(ms for ms, _ in timed)
+    return next(t for ms, t in timed if ms <= 1.01 * fastest), times
 
 
 def run_ours(args, dist: Dist):
