@@ -247,6 +247,23 @@ SARBP_API int sarbp_upload_raw_bins(void *dst, int64_t dst_pitch, const void *sr
                                     int64_t npulses, void *stream);
 
 /*
+ * The same copies done by SM loads instead of a copy engine, for callers
+ * whose latency depends on their uploads: on the GB300 machines this library is
+ * measured on, copy-engine host-to-device transfers stall for 10-100 ms every
+ * so often while kernels reading the same memory over the CPU-GPU link did
+ * not (at ~90 % of the copy engine's bandwidth).  `src` must be page-locked
+ * host memory mapped into the device's address space (cudaHostAlloc, torch
+ * pin_memory) or device memory, else SARBP_EINVAL before any launch.
+ * sarbp_upload_raw_bins_sm takes sarbp_upload_raw_bins's arguments;
+ * sarbp_copy_to_device_sm copies `bytes` bytes.  Stream-ordered, no
+ * synchronisation.  No reference counterpart.
+ */
+SARBP_API int sarbp_upload_raw_bins_sm(void *dst, int64_t dst_pitch, const void *src,
+                                       int64_t src_pitch, int64_t bin_lo, int64_t nbins,
+                                       int64_t npulses, void *stream);
+SARBP_API int sarbp_copy_to_device_sm(void *dst, const void *src, int64_t bytes, void *stream);
+
+/*
  * Batches: many scenes of uneven size in one persistent launch.
  * Replaces the reference's per-batch host loops (gpu_small_dataset.py:285-339,
  * main_gpu.py:415-586), which launch one kernel per pixel batch and copy

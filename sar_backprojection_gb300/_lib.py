@@ -92,6 +92,9 @@ SIGNATURES = {
                                             C.c_size_t, _P, _P]),
     "sarbp_upload_raw_bins": (C.c_int, [_P, C.c_int64, _P, C.c_int64, C.c_int64, C.c_int64,
                                         C.c_int64, _P]),
+    "sarbp_upload_raw_bins_sm": (C.c_int, [_P, C.c_int64, _P, C.c_int64, C.c_int64,
+                                           C.c_int64, C.c_int64, _P]),
+    "sarbp_copy_to_device_sm": (C.c_int, [_P, _P, C.c_int64, _P]),
     "sarbp_focus_mixed_noalloc": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, _P, _P,
                                             _P, _P]),
     "sarbp_tile_count": (C.c_int64, [C.POINTER(Scene), C.POINTER(Tuning)]),

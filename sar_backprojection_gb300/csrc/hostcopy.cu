@@ -1,0 +1,148 @@
+// hostcopy.cu -- host-to-device copies done by SM loads instead of a copy
+// engine.
+//
+// On the GB300 machines this library is measured on, copy-engine transfers from
+// page-locked host memory stall for 10-100 ms every so often (about every
+// 0.5 s under a steady load), while kernels reading the same memory through
+// its mapped device address over the CPU-GPU link ran without a stall in
+// every measurement (at 185-190 GB/s against the copy engine's ~205 GB/s).
+// A caller that mostly waits on uploads rather than on kernels (the serving
+// loop) gets a steadier latency from these copies.  The source must be
+// page-locked host memory mapped into the device's address space (what
+// cudaHostAlloc / torch pin_memory give) or device memory; anything else is
+// rejected before any launch.
+#include "sarbp_internal.cuh"
+
+namespace sarbp {
+
+// Device address of `src` for kernel loads, or nullptr when the memory is
+// not page-locked host memory with a mapping (or device memory).
+static const void *device_view(const void *src)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, src) != cudaSuccess) {
+        cudaGetLastError();   // clear the sticky-free error of an unknown pointer
+        return nullptr;
+    }
+    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged)
+        return src;
+    if (at.type == cudaMemoryTypeHost) return at.devicePointer;
+    return nullptr;
+}
+
+constexpr int kCopyThreads = 256;
+constexpr int kCopyUnroll = 4;
+
+// dst[r*dpitch + lo + i] = src[r*spitch + lo + i], i < n, r < rows (complex64).
+__global__ void __launch_bounds__(kCopyThreads)
+gather_rows_kernel(float2 *__restrict__ dst, int64_t dpitch, const float2 *__restrict__ src,
+                   int64_t spitch, int64_t lo, int64_t n, int64_t rows)
+{
+    for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        const float2 *s = src + r * spitch + lo;
+        float2 *d = dst + r * dpitch + lo;
+        for (int64_t i = threadIdx.x; i < n; i += (int64_t)kCopyUnroll * kCopyThreads) {
+            float2 v[kCopyUnroll];
+#pragma unroll
+            for (int u = 0; u < kCopyUnroll; ++u) {
+                const int64_t k = i + (int64_t)u * kCopyThreads;
+                if (k < n) v[u] = s[k];
+            }
+#pragma unroll
+            for (int u = 0; u < kCopyUnroll; ++u) {
+                const int64_t k = i + (int64_t)u * kCopyThreads;
+                if (k < n) d[k] = v[u];
+            }
+        }
+    }
+}
+
+// Byte copy: 16-byte words when both ends share their alignment mod 16, the
+// unaligned head and the tail byte by byte.
+__global__ void __launch_bounds__(kCopyThreads)
+copy_bytes_kernel(unsigned char *__restrict__ dst, const unsigned char *__restrict__ src,
+                  int64_t bytes, int64_t head, int64_t nvec)
+{
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src + head);
+    uint4 *d4 = reinterpret_cast<uint4 *>(dst + head);
+    for (int64_t i = tid; i < nvec; i += kCopyUnroll * stride) {
+        uint4 v[kCopyUnroll];
+#pragma unroll
+        for (int u = 0; u < kCopyUnroll; ++u)
+            if (i + u * stride < nvec) v[u] = s4[i + u * stride];
+#pragma unroll
+        for (int u = 0; u < kCopyUnroll; ++u)
+            if (i + u * stride < nvec) d4[i + u * stride] = v[u];
+    }
+    const int64_t tail = head + nvec * 16;
+    for (int64_t i = tid; i < head; i += stride) dst[i] = src[i];
+    for (int64_t i = tail + tid; i < bytes; i += stride) dst[i] = src[i];
+}
+
+static int copy_grid(int64_t work_units)
+{
+    int dev = 0, sms = 148;
+    if (cudaGetDevice(&dev) == cudaSuccess)
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t g = 2LL * sms;
+    return (int)(work_units < g ? (work_units > 0 ? work_units : 1) : g);
+}
+
+}  // namespace sarbp
+
+using namespace sarbp;
+
+extern "C" SARBP_API int sarbp_upload_raw_bins_sm(void *dst, int64_t dst_pitch, const void *src,
+                                                  int64_t src_pitch, int64_t bin_lo,
+                                                  int64_t nbins, int64_t npulses, void *stream)
+{
+    if (!dst || !src || dst_pitch <= 0 || src_pitch <= 0 || bin_lo < 0 || nbins < 0 ||
+        npulses < 0 || bin_lo + nbins > dst_pitch || bin_lo + nbins > src_pitch) {
+        set_error("sarbp_upload_raw_bins_sm: bad pointers or bin range [%lld, +%lld) for "
+                  "pitches %lld / %lld",
+                  (long long)bin_lo, (long long)nbins, (long long)dst_pitch,
+                  (long long)src_pitch);
+        return SARBP_EINVAL;
+    }
+    if (nbins == 0 || npulses == 0) return SARBP_OK;
+    const void *sv = device_view(src);
+    if (!sv) {
+        set_error("sarbp_upload_raw_bins_sm: the source is not page-locked host memory mapped "
+                  "into the device's address space (or device memory)");
+        return SARBP_EINVAL;
+    }
+    gather_rows_kernel<<<copy_grid(npulses), kCopyThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<float2 *>(dst), dst_pitch, static_cast<const float2 *>(sv), src_pitch, bin_lo,
+        nbins, npulses);
+    return cuda_status(cudaGetLastError(), "sarbp_upload_raw_bins_sm launch");
+}
+
+extern "C" SARBP_API int sarbp_copy_to_device_sm(void *dst, const void *src, int64_t bytes,
+                                                 void *stream)
+{
+    if (!dst || !src || bytes < 0) {
+        set_error("sarbp_copy_to_device_sm: bad pointers or size %lld", (long long)bytes);
+        return SARBP_EINVAL;
+    }
+    if (bytes == 0) return SARBP_OK;
+    const void *sv = device_view(src);
+    if (!sv) {
+        set_error("sarbp_copy_to_device_sm: the source is not page-locked host memory mapped "
+                  "into the device's address space (or device memory)");
+        return SARBP_EINVAL;
+    }
+    const uintptr_t sa = reinterpret_cast<uintptr_t>(sv), da = reinterpret_cast<uintptr_t>(dst);
+    int64_t head = bytes, nvec = 0;               // all bytes one by one ...
+    if ((sa & 15) == (da & 15)) {                 // ... unless the ends align alike
+        head = (int64_t)((16 - (sa & 15)) & 15);
+        if (head > bytes) head = bytes;
+        nvec = (bytes - head) / 16;
+    }
+    copy_bytes_kernel<<<copy_grid((nvec + kCopyThreads - 1) / kCopyThreads + 1), kCopyThreads, 0,
+                        static_cast<cudaStream_t>(stream)>>>(
+        static_cast<unsigned char *>(dst), static_cast<const unsigned char *>(sv), bytes, head,
+        nvec);
+    return cuda_status(cudaGetLastError(), "sarbp_copy_to_device_sm launch");
+}

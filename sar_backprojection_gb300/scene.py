@@ -34,14 +34,27 @@ def _cast_host(a, np_dtype):
     return a if a.dtype == np_dtype else a.astype(np_dtype)
 
 
-def flatten_f(a, np_dtype, device) -> torch.Tensor:
+def _to_device(t: torch.Tensor, device, sm: bool) -> torch.Tensor:
+    """Host tensor -> device tensor on the current stream; with ``sm`` a
+    contiguous page-locked source is copied by SM loads
+    (sarbp_copy_to_device_sm) instead of a copy engine."""
+    if sm and t.device.type == "cpu" and t.is_contiguous() and t.is_pinned():
+        d = torch.empty(t.shape, dtype=t.dtype, device=device)
+        _lib.check(_lib.load().sarbp_copy_to_device_sm(
+            d.data_ptr(), t.data_ptr(), t.numel() * t.element_size(),
+            torch.cuda.current_stream(d.device).cuda_stream))
+        return d
+    return t.to(device, non_blocking=True)
+
+
+def flatten_f(a, np_dtype, device, sm: bool = False) -> torch.Tensor:
     """``a.astype(dtype).flatten(order='F')`` as a contiguous device tensor."""
     a = _cast_host(a, np_dtype)
     t = _as_tensor(a)
     if t.dim() > 1:
         # C-order flatten of the axis-reversed array == F-order flatten
         t = t.permute(*reversed(range(t.dim())))
-    t = t.to(device, non_blocking=True)
+    t = _to_device(t, device, sm)
     return t.contiguous().view(-1)
 
 
@@ -229,7 +242,8 @@ def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
                     near_range, dra, lambda_val, Sint, device=None,
                     raw_bins: str = "all", tuning=None,
                     raw_buffer: torch.Tensor | None = None,
-                    bound_host: torch.Tensor | None = None) -> DeviceScene:
+                    bound_host: torch.Tensor | None = None,
+                    h2d: str = "copy") -> DeviceScene:
     """Upload the reference's 13 focusing arguments (same order) to the device.
 
     Raises ValueError where the reference does (Raw_Data or xxg1 not 2-D,
@@ -251,7 +265,12 @@ def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
     ``raw_buffer``: a float32 (Naz, pitch, 2) device tensor to receive the
     raw rows in those modes instead of a new allocation (the caller owns
     its reuse).
+    ``h2d="sm"``: page-locked host inputs other than the raw rows are copied
+    by SM loads instead of a copy engine (``sarbp_copy_to_device_sm``).
     """
+    if h2d not in ("copy", "sm"):
+        raise ValueError(f"h2d must be 'copy' or 'sm', got {h2d!r}")
+    sm = h2d == "sm"
     if raw_bins not in ("all", "reached", "bound", "deferred"):
         raise ValueError("raw_bins must be 'all', 'reached', 'bound' or 'deferred', "
                          f"got {raw_bins!r}")
@@ -291,14 +310,14 @@ def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
 
     def traj(w):
         t = _as_tensor(_cast_host(w, np.float64)).reshape(-1)
-        return t.to(device, non_blocking=True).contiguous()
+        return _to_device(t, device, sm).contiguous()
 
     scene = DeviceScene(
         dim0=dim0, dim1=dim1,
-        x=flatten_f(xxg1, np.float64, device), y=flatten_f(yyg1, np.float64, device),
-        z=flatten_f(zzg1, np.float64, device),
-        mask=flatten_f(mask, np.uint8, device), index=flatten_f(index, np.int32, device),
-        sint=flatten_f(Sint, np.int32, device),
+        x=flatten_f(xxg1, np.float64, device, sm), y=flatten_f(yyg1, np.float64, device, sm),
+        z=flatten_f(zzg1, np.float64, device, sm),
+        mask=flatten_f(mask, np.uint8, device, sm), index=flatten_f(index, np.int32, device, sm),
+        sint=flatten_f(Sint, np.int32, device, sm),
         tx=traj(wgsx), ty=traj(wgsy), tz=traj(wgsz),
         raw=raw_t, nra=nra, naz=naz, pitch=pitch,
         near_range=float(near_range), delta_range=float(dra), lambda_=float(lambda_val),

@@ -10,7 +10,8 @@ Requests (focusing jobs of different sizes) arrive over time.  The engine
   stream order, and on a later pass, once the host sees it, only the range
   bins the job's apertures can reach are copied from host raw data on the
   copy stream (the job's raw data and trajectory stay resident until it
-  finishes);
+  finishes); page-locked inputs go up by SM loads (``h2d="sm"``), which
+  on this hardware do not share the copy engine's occasional stalls;
 * runs the device in *waves*: each wave is one launch of the persistent
   batch kernel whose work queue holds pixel tiles of every resident job (one
   whose raw copy the host has seen complete), so a job that arrives while
@@ -121,7 +122,8 @@ class ServingEngine:
     """Continuous batching of focusing jobs on one device (see module doc)."""
 
     def __init__(self, device=None, budget_bytes: int = 150 * GB, max_slots: int = 32,
-                 wave_items: int | None = None, tuning=None, policy: str = "fifo"):
+                 wave_items: int | None = None, tuning=None, policy: str = "fifo",
+                 h2d: str = "sm"):
         self.device = torch.device(device or "cuda")
         self.lib = _lib.load()
         self.tuning = staged_tuning() if tuning is None else resolve_tuning(tuning)
@@ -131,7 +133,13 @@ class ServingEngine:
         self.wave_items = int(wave_items or 3 * 2 * props.multi_processor_count)
         if policy not in ("fifo", "srpt"):
             raise ValueError("policy must be 'fifo' or 'srpt'")
+        if h2d not in ("copy", "sm"):
+            raise ValueError("h2d must be 'copy' or 'sm'")
         self.policy = policy
+        # page-locked job inputs go up by SM loads ("sm", sarbp_*_sm): the
+        # copy engine's host-to-device transfers stall now and then on this
+        # hardware and every job queued behind a stall waits; "copy" uses it
+        self.h2d = h2d
         self.compute = [torch.cuda.Stream(self.device), torch.cuda.Stream(self.device)]
         self.setup = torch.cuda.Stream(self.device)      # small inputs, tables, bound
         self.copy = torch.cuda.Stream(self.device)       # raw range bins
@@ -158,7 +166,8 @@ class ServingEngine:
             # batch scene slot, all queued on the setup stream: nothing here
             # waits for the GPU
             scene = scene_to_device(*job.args, device=self.device, raw_bins="deferred",
-                                    tuning=self.tuning, bound_host=self.bounds[slot])
+                                    tuning=self.tuning, bound_host=self.bounds[slot],
+                                    h2d=self.h2d)
             ws_bytes = _lib.check(int(self.lib.sarbp_mixed_workspace_size(
                 C.byref(scene.struct()), tb)))
             out = torch.empty((scene.npix, 2), dtype=torch.float64, device=self.device)
@@ -192,9 +201,11 @@ class ServingEngine:
             lo, hi = read_bound(scene)
             if hi >= lo:
                 n = hi - lo + 1
-                _lib.check(self.lib.sarbp_upload_raw_bins(
-                    scene.raw.data_ptr(), scene.pitch, scene.host_rows.data_ptr(), scene.nra,
-                    lo, n, scene.naz, self.copy.cuda_stream))
+                upload = (self.lib.sarbp_upload_raw_bins_sm
+                          if self.h2d == "sm" and scene.host_rows.is_pinned()
+                          else self.lib.sarbp_upload_raw_bins)
+                _lib.check(upload(scene.raw.data_ptr(), scene.pitch, scene.host_rows.data_ptr(),
+                                  scene.nra, lo, n, scene.naz, self.copy.cuda_stream))
                 scene.h2d_bytes += n * scene.naz * 8
         a.uploaded = torch.cuda.Event()
         a.uploaded.record(self.copy)

@@ -125,6 +125,19 @@ def test_new_entry_points_reject_bad_arguments_without_a_gpu():
     # zero bins or pulses: nothing to do
     assert lib.sarbp_upload_raw_bins(C.c_void_p(0x1000), 100, C.c_void_p(0x2000), 100, 0, 0,
                                      5, None) == _lib.SARBP_OK
+    # the SM-load variants check the same arguments before touching the GPU
+    assert lib.sarbp_upload_raw_bins_sm(C.c_void_p(0x1000), 100, C.c_void_p(0x2000), 100, 90,
+                                        20, 5, None) == _lib.SARBP_EINVAL
+    assert "bin range" in _lib.last_error()
+    assert lib.sarbp_upload_raw_bins_sm(None, 100, C.c_void_p(0x2000), 100, 0, 10, 5,
+                                        None) == _lib.SARBP_EINVAL
+    assert lib.sarbp_upload_raw_bins_sm(C.c_void_p(0x1000), 100, C.c_void_p(0x2000), 100, 0,
+                                        0, 5, None) == _lib.SARBP_OK
+    assert lib.sarbp_copy_to_device_sm(None, C.c_void_p(0x2000), 16, None) == _lib.SARBP_EINVAL
+    assert lib.sarbp_copy_to_device_sm(C.c_void_p(0x1000), C.c_void_p(0x2000), -1,
+                                       None) == _lib.SARBP_EINVAL
+    assert lib.sarbp_copy_to_device_sm(C.c_void_p(0x1000), C.c_void_p(0x2000), 0,
+                                       None) == _lib.SARBP_OK
     s = _lib.Scene()
     s.dim0, s.dim1 = 64, 16
     for f in ("dem_x", "dem_y", "dem_z", "mask", "index", "sint", "traj_x", "traj_y",

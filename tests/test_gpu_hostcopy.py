@@ -1,0 +1,95 @@
+"""Host-to-device copies by SM loads (sarbp_upload_raw_bins_sm,
+sarbp_copy_to_device_sm) give the copy engine's bytes, reject memory the
+device cannot load from, and the serving engine that uses them for pinned
+job inputs still gives every job the image it gets alone."""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from sar_backprojection_gb300 import _lib, batch, focus, scene_to_device, serve, synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.set_device(0)
+    return _lib.load()
+
+
+def _stream():
+    return torch.cuda.current_stream().cuda_stream
+
+
+def test_raw_bins_match_the_copy_engine(lib):
+    naz, nra, lo, nb = 257, 1001, 123, 517          # odd pitch and offsets
+    host = torch.randn((naz, nra, 2), dtype=torch.float32).pin_memory()
+    a = torch.full((naz, nra + 1, 2), 7.0, device="cuda")
+    b = a.clone()
+    _lib.check(lib.sarbp_upload_raw_bins(a.data_ptr(), nra + 1, host.data_ptr(), nra, lo, nb,
+                                         naz, _stream()))
+    _lib.check(lib.sarbp_upload_raw_bins_sm(b.data_ptr(), nra + 1, host.data_ptr(), nra, lo, nb,
+                                            naz, _stream()))
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+    assert torch.equal(b[:, lo:lo + nb].cpu(), host[:, lo:lo + nb])
+    assert bool((b[:, :lo] == 7.0).all()) and bool((b[:, lo + nb:] == 7.0).all())
+
+
+@pytest.mark.parametrize("offset,size", [(0, 0), (0, 1), (3, 5), (5, 4096), (16, 1 << 20),
+                                         (7, (1 << 20) + 13), (0, 3_000_001)])
+def test_bytes_match(lib, offset, size):
+    src = torch.randint(0, 256, (size + 64,), dtype=torch.uint8).pin_memory()
+    dst = torch.zeros(size + 64, dtype=torch.uint8, device="cuda")
+    for dofs in (0, 1, offset % 16):
+        dst.zero_()
+        _lib.check(lib.sarbp_copy_to_device_sm(dst.data_ptr() + dofs, src.data_ptr() + offset,
+                                               size, _stream()))
+        torch.cuda.synchronize()
+        got = dst.cpu()
+        assert torch.equal(got[dofs:dofs + size], src[offset:offset + size])
+        assert int(got[:dofs].sum()) == 0 and int(got[dofs + size:].sum()) == 0
+
+
+def test_pageable_source_is_rejected(lib):
+    src = np.zeros(4096, dtype=np.uint8)                 # not page-locked
+    dst = torch.zeros(4096, dtype=torch.uint8, device="cuda")
+    rc = lib.sarbp_copy_to_device_sm(dst.data_ptr(), src.ctypes.data, 4096, _stream())
+    assert rc == _lib.SARBP_EINVAL and "page-locked" in _lib.last_error()
+    rc = lib.sarbp_upload_raw_bins_sm(dst.data_ptr(), 64, src.ctypes.data, 64, 0, 8, 8,
+                                      _stream())
+    assert rc == _lib.SARBP_EINVAL
+
+
+def _pinned_args(sc):
+    args = list(synth.focus_args(sc))
+    for i in (0, 1, 2, 3, 4, 5, 6, 7, 8, 12):
+        a = np.asarray(args[i])
+        t = torch.from_numpy(np.ascontiguousarray(a.T) if a.ndim == 2 else a)
+        args[i] = t.pin_memory().t() if a.ndim == 2 else t.pin_memory()
+    return tuple(args)
+
+
+def test_serving_with_pinned_inputs_matches_alone(lib):
+    sizes = [(128, 32, 2001, 200, 260), (96, 40, 2401, 900, 1300), (160, 64, 3001, 600, 800)]
+    arrivals = serve.poisson_arrivals(6, rate_per_s=400.0, seed=5)
+    jobs = []
+    for i in range(6):
+        d0, d1, naz, s_lo, s_hi = sizes[i % 3]
+        sc = synth.generate(synth.scaled_full(300 + i, d0, d1, naz, s_lo, s_hi))
+        jobs.append(serve.Job(job_id=i, args=_pinned_args(sc), arrival=float(arrivals[i])))
+    tuning = batch.staged_tuning()
+    rep = serve.ServingEngine(budget_bytes=8 * serve.GB, max_slots=4, wave_items=64,
+                              tuning=tuning).run(jobs)
+    assert rep.summary()["completed"] == len(jobs)
+    for j in jobs:
+        ds = scene_to_device(*j.args, device="cuda")
+        alone = focus(ds, "mixed", tuning=tuning)
+        torch.cuda.synchronize()
+        ref = alone.to_numpy(ds.dim0, ds.dim1)
+        assert np.array_equal(np.ascontiguousarray(j.image).view(np.uint64),
+                              np.ascontiguousarray(ref).view(np.uint64)), f"job {j.job_id}"
