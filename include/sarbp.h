@@ -277,13 +277,17 @@ SARBP_API int sarbp_copy_to_device_sm(void *dst, const void *src, int64_t bytes,
  * sarbp_batch_workspace_size: bytes of the batch workspace (scene
  *   descriptors + queue) for `nscenes` scenes and up to `max_items` items.
  * sarbp_batch_set_scene: describe scene `slot` (its mixed workspace must be
- *   prepared with sarbp_mixed_prepare under the same tuning).
+ *   prepared with sarbp_mixed_prepare under the same tuning); the descriptor
+ *   is written in stream order by a kernel that receives it as a parameter,
+ *   so the host never waits.
  * sarbp_batch_set_items: upload the queue, `n_items` (scene slot, tile index)
- *   int32 pairs in processing order (decreasing cost balances the load).
+ *   int32 pairs in processing order (decreasing cost balances the load); from
+ *   pageable host memory the copy first waits for `stream`.
  * sarbp_batch_focus: reset the queue cursor and launch the persistent kernel;
  *   stream-ordered, no host synchronisation, capturable in a CUDA graph.
  *   `diagnostics` != 0 also writes the scenes' checksum outputs.
- * The batch path needs the staged kernel (tuning.staged = 1, chunk 32).
+ * The batch path needs the staged kernel (tuning.staged = 1; 32-, 64- or
+ * 128-pulse chunks).
  */
 SARBP_API int64_t sarbp_tile_count(const sarbp_scene *scene, const sarbp_tuning *tuning);
 SARBP_API int sarbp_tile_costs(const sarbp_scene *scene, const sarbp_tuning *tuning,
