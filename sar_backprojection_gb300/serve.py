@@ -124,6 +124,10 @@ class ServingEngine:
     def __init__(self, device=None, budget_bytes: int = 150 * GB, max_slots: int = 32,
                  wave_items: int | None = None, tuning=None, policy: str = "fifo",
                  h2d: str = "sm"):
+        if policy not in ("fifo", "srpt"):
+            raise ValueError("policy must be 'fifo' or 'srpt'")
+        if h2d not in ("copy", "sm"):
+            raise ValueError("h2d must be 'copy' or 'sm'")
         self.device = torch.device(device or "cuda")
         self.lib = _lib.load()
         self.tuning = staged_tuning() if tuning is None else resolve_tuning(tuning)
@@ -131,10 +135,6 @@ class ServingEngine:
         self.max_slots = int(max_slots)
         props = torch.cuda.get_device_properties(self.device)
         self.wave_items = int(wave_items or 3 * 2 * props.multi_processor_count)
-        if policy not in ("fifo", "srpt"):
-            raise ValueError("policy must be 'fifo' or 'srpt'")
-        if h2d not in ("copy", "sm"):
-            raise ValueError("h2d must be 'copy' or 'sm'")
         self.policy = policy
         # page-locked job inputs go up by SM loads ("sm", sarbp_*_sm): the
         # copy engine's host-to-device transfers stall now and then on this

@@ -84,3 +84,40 @@ def test_host_image_pool_reuses_only_unreferenced_arrays():
     held = [pool.get(2, 2) for _ in range(IMAGE_POOL + 2)]
     assert len({id(x) for x in held}) == len(held)
     assert len(pool.arrays) <= IMAGE_POOL
+
+
+def test_scene_upload_mode_arguments_are_checked_before_the_device():
+    from sar_backprojection_gb300.scene import scene_to_device
+    a = _args()
+    with pytest.raises(ValueError, match="raw_bins"):
+        scene_to_device(*a, raw_bins="sometimes")
+    with pytest.raises(ValueError, match="bound_host"):
+        scene_to_device(*a, raw_bins="deferred")          # needs the pinned pair
+    with pytest.raises(ValueError, match="h2d"):
+        scene_to_device(*a, h2d="dma")
+
+
+def test_read_bound_takes_the_deferred_pair_once():
+    """read_bound turns the pair the device wrote into (bin_lo, bin_hi) and
+    forgets the buffer, so a later call returns the same values."""
+    from types import SimpleNamespace
+    from sar_backprojection_gb300.scene import read_bound
+    pair = torch.tensor([209, 1785], dtype=torch.int32)
+    sc = SimpleNamespace(bound_host=pair, bin_lo=0, bin_hi=-1)
+    assert read_bound(sc) == (209, 1785)
+    assert sc.bound_host is None
+    pair[:] = torch.tensor([1, 0], dtype=torch.int32)      # the slot's next job
+    assert read_bound(sc) == (209, 1785)
+    empty = SimpleNamespace(bound_host=torch.tensor([1, 0], dtype=torch.int32), bin_lo=0,
+                            bin_hi=-1)
+    lo, hi = read_bound(empty)
+    assert lo > hi                                           # nothing reached
+
+
+
+def test_serving_engine_checks_its_options_before_the_device():
+    from sar_backprojection_gb300 import serve
+    with pytest.raises(ValueError, match="h2d"):
+        serve.ServingEngine(device="cpu", h2d="dma")
+    with pytest.raises(ValueError, match="policy"):
+        serve.ServingEngine(device="cpu", policy="lifo")
