@@ -140,8 +140,12 @@ extern "C" SARBP_API int sarbp_copy_to_device_sm(void *dst, const void *src, int
         if (head > bytes) head = bytes;
         nvec = (bytes - head) / 16;
     }
-    copy_bytes_kernel<<<copy_grid((nvec + kCopyThreads - 1) / kCopyThreads + 1), kCopyThreads, 0,
-                        static_cast<cudaStream_t>(stream)>>>(
+    // CTAs for the 16-byte words and for the bytes copied one by one (all of
+    // them when the ends are not aligned alike), 16 per thread
+    const int64_t singles = bytes - nvec * 16;
+    const int64_t units = (nvec + kCopyThreads - 1) / kCopyThreads +
+                          (singles + 16 * kCopyThreads - 1) / (16 * kCopyThreads);
+    copy_bytes_kernel<<<copy_grid(units), kCopyThreads, 0, static_cast<cudaStream_t>(stream)>>>(
         static_cast<unsigned char *>(dst), static_cast<const unsigned char *>(sv), bytes, head,
         nvec);
     return cuda_status(cudaGetLastError(), "sarbp_copy_to_device_sm launch");
