@@ -228,6 +228,23 @@ def pick_sample(host_scene, raw_prepared, nthreads, seconds, rng):
     return pix, work
 
 
+def reference_timing() -> dict | None:
+    """The reference's own focusing call timed where its source is available
+    (tests/golden/reference_timing.json, written by tests/golden/make_golden.py):
+    one core, NumPy interpreting the Numba-decorated loop (no Numba there), on
+    the build container's CPU, not this host."""
+    path = Path(__file__).resolve().parent / "tests" / "golden" / "reference_timing.json"
+    try:
+        t = json.loads(path.read_text())
+    except (OSError, ValueError):
+        return None
+    t["unit"] = UNIT
+    t["value"] = t.pop("gpix_pulse_per_s")
+    t["note"] = ("measured in the build container, not on this host; Numba's JIT is absent "
+                 "there, so the loop runs as plain NumPy")
+    return t
+
+
 def host_scene_of(scene: dict) -> dict:
     h = dict(scene)
     raw = scene["RawData"]
@@ -625,7 +642,8 @@ def run_ours(args, dist: Dist):
         dt = oracle_sample_run(host_sc, raw_prepared, pix, cores)
         cpu = {"value": w_s / dt / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{pix.size} of {ds.npix} pixels (seeded uniform), {w_s} pixel-pulses, "
-                         f"{dt:.1f} s"}
+                         f"{dt:.1f} s",
+               "reference_as_is": reference_timing()}
 
     if dist.rank == 0:
         line = {

@@ -19,15 +19,21 @@ Fixtures written (all .npz):
                        bins across 0 and Nra-2..Nra): inputs and image stored.
   golden_ties.npz   -- exact .5 range-bin ties (half-to-even rounding):
                        inputs and image stored.
+  reference_timing.json -- wall time of the reference call on the small
+                       workload (one core, NumPy under the numba stub), with
+                       the host it ran on: the reference's own CPU speed,
+                       which cannot be measured where the reference is absent.
 
-Usage: python tests/golden/make_golden.py [--only small|edges|ties]
+Usage: python tests/golden/make_golden.py [--only small|edges|ties|timing]
 """
 from __future__ import annotations
 
 import contextlib
 import importlib.util
 import io
+import json
 import os
+import platform
 import sys
 import tempfile
 import time
@@ -159,14 +165,25 @@ INPUT_KEYS = ("xxg1", "yyg1", "zzg1", "Mask", "Index", "Sint", "wgsx", "wgsy", "
 def main(argv):
     only = argv[argv.index("--only") + 1] if "--only" in argv else None
     mod = load_reference()
-    if only in (None, "small"):
+    if only in (None, "small", "timing"):
         spec = synth.config_small()
         scene = synth.generate(spec)
-        t = time.time()
+        t = time.perf_counter()
         img = run_reference(mod, scene)
-        print(f"small: reference took {time.time() - t:.1f} s")
-        np.savez_compressed(HERE / "golden_small.npz", seed=spec.seed,
-                            digest=synth.input_digest(scene), image=img)
+        seconds = time.perf_counter() - t
+        print(f"small: reference took {seconds:.1f} s")
+        if only != "timing":
+            np.savez_compressed(HERE / "golden_small.npz", seed=spec.seed,
+                                digest=synth.input_digest(scene), image=img)
+        work = synth.nominal_pixel_pulses(scene)
+        (HERE / "reference_timing.json").write_text(json.dumps({
+            "workload": "small: DEM 256x64, 2001 pulses, Sint 400",
+            "nominal_pixel_pulses": int(work), "seconds": round(seconds, 3),
+            "gpix_pulse_per_s": work / seconds / 1e9, "cores": 1,
+            "implementation": "reference FocalizzatoreBpPx (sar_focuser_puntual_noui.py:149), "
+                              "unmodified, numba stub (plain NumPy)",
+            "host": f"{platform.machine()} {platform.processor() or ''}".strip(),
+            "numpy": np.__version__}, indent=1) + "\n")
     for name, make in (("edges", edges_scene), ("ties", ties_scene)):
         if only not in (None, name):
             continue
