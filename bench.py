@@ -290,7 +290,7 @@ def run_reference(args, dist: Dist):
                                      "FocalizzatoreBpPx, OpenMP over pixels",
                    "l2": "host run (no GPU)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, "reference_as_is": reference_timing()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
     }
