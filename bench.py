@@ -441,8 +441,14 @@ def pick_tuning(lib, ds, dev, candidates=AUTOTUNE_CANDIDATES, reps: int = 5):
         times[",".join(map(str, cand))] = round(ms, 4)
         timed.append((ms, t))
         del ws
+    return choose_tuning(timed), times
+
+
+def choose_tuning(timed, tolerance: float = 0.01):
+    """The first (ms, tuning) pair, in the candidates' order of preference,
+    within ``tolerance`` of the fastest."""
     fastest = min(ms for ms, _ in timed)
-    return next(t for ms, t in timed if ms <= 1.01 * fastest), times
+    return next(t for ms, t in timed if ms <= (1.0 + tolerance) * fastest)
 
 
 def run_ours(args, dist: Dist):

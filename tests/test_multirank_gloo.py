@@ -52,3 +52,11 @@ def test_two_gloo_ranks():
     assert [r[0] for r in res] == [0, 1]
     assert res[0][1] != res[1][1]               # one distinct scene per rank
     assert res[0][2] == res[1][2] == 11.0       # max over ranks
+
+
+def test_autotuner_prefers_earlier_candidates_within_noise():
+    import bench
+    # 208-bin window listed first: kept when a later candidate wins by < 1 %
+    assert bench.choose_tuning([(1.7174, "w208"), (1.7681, "c64"), (1.7161, "w192")]) == "w208"
+    assert bench.choose_tuning([(1.80, "w208"), (1.70, "w192")]) == "w192"
+    assert bench.choose_tuning([(2.0, "a")]) == "a"
