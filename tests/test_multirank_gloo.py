@@ -1,4 +1,5 @@
-"""bench.py's multi-rank bookkeeping on CPU: two gloo ranks, one scene each.
+"""bench.py's host logic on CPU: the multi-rank bookkeeping (two gloo ranks,
+one scene each) and the autotuner's choice among timed candidates.
 
 The focusing path shards by scene (weak scaling, no collective on the data
 path); the only cross-rank operations are the barrier around the timed
