@@ -315,11 +315,14 @@ SARBP_API int sarbp_batch_focus(void *batch_ws, size_t batch_bytes, int32_t nsce
  * library-owned device array of about 7 MiB, sized for scenes of at most
  * SARBP_NOALLOC_MAX_PULSES pulses (larger scenes are rejected with
  * SARBP_ERANGE), which every GPU that loads the library keeps until the
- * process exits.  The first call on a device looks up the array's device
- * address on that device, so make it before any stream capture.  Every call
- * shares the one array: calls whose work overlaps on the GPU (different
- * streams, or other host threads) race and must be serialised by the caller.
- * Calls no cudaMalloc/cudaFree.
+ * process exits.  The first call in a device's CUDA context looks up the
+ * array's device address in that context, so make it before any stream
+ * capture.  Every call shares the one array: calls whose work overlaps on
+ * the GPU (different streams, or other host threads) race and must be
+ * serialised by the caller.  Unlike sarbp_focus_mixed this call waits for
+ * `stream` before it returns: it reads the array's status block back and
+ * returns SARBP_ETIMEOUT when a bounded device wait gave up (the image is
+ * then incomplete).  Calls no cudaMalloc/cudaFree.
  */
 #define SARBP_NOALLOC_MAX_PULSES 131072
 SARBP_API int sarbp_focus_mixed_noalloc(const sarbp_scene *scene,

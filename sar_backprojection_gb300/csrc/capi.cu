@@ -156,6 +156,18 @@ bool valid_tuning(sarbp_tuning *t)
     return true;
 }
 
+// Clear the thread's error, validate the scene and the tuning.
+int mixed_args(const sarbp_scene *scene, const sarbp_tuning *tuning, SceneParams *P,
+               sarbp_tuning *T)
+{
+    g_last_error[0] = 0;
+    if (!build_params(scene, P)) return SARBP_EINVAL;
+    *T = sarbp_tuning{};
+    if (tuning) *T = *tuning;
+    if (!valid_tuning(T)) return SARBP_EINVAL;
+    return SARBP_OK;
+}
+
 }  // namespace sarbp
 
 using namespace sarbp;
@@ -201,16 +213,6 @@ SARBP_API int64_t sarbp_mixed_workspace_size(const sarbp_scene *scene, const sar
     return (int64_t)mixed_layout(P, T).total;
 }
 
-static int mixed_args(const sarbp_scene *scene, const sarbp_tuning *tuning, SceneParams *P,
-                      sarbp_tuning *T)
-{
-    g_last_error[0] = 0;
-    if (!build_params(scene, P)) return SARBP_EINVAL;
-    *T = sarbp_tuning{};
-    if (tuning) *T = *tuning;
-    if (!valid_tuning(T)) return SARBP_EINVAL;
-    return SARBP_OK;
-}
 
 SARBP_API int sarbp_mixed_prepare(const sarbp_scene *scene, const sarbp_tuning *tuning,
                                   void *workspace, size_t workspace_bytes, void *stream)

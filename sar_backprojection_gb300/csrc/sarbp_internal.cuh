@@ -142,6 +142,9 @@ void set_error(const char *fmt, ...);
 bool build_params(const sarbp_scene *s, SceneParams *p);
 int cuda_status(cudaError_t e, const char *what);
 bool valid_tuning(sarbp_tuning *t);   // fills library defaults, validates
+// Clear the thread's error, validate the scene and the tuning (defaults filled).
+int mixed_args(const sarbp_scene *scene, const sarbp_tuning *tuning, SceneParams *P,
+               sarbp_tuning *T);
 
 // Mixed-path workspace layout (offsets 256-byte aligned).  The first part
 // (up to `base`) is the chunk tables every mixed launch needs; staged=2

@@ -11,12 +11,30 @@
   so that the mask does not depend on the image's scale.
 
 ``python -m sar_backprojection_gb300.quality a.dat b.dat --shape D0 D1``
-compares two images stored as interleaved complex128 (.dat) or .npy files.
+(or the reference tool's spelling, ``--file1 a.dat --file2 b.dat --shape
+D0,D1 --fmt1 split --fmt2 truth``) compares two images and prints the
+statistics as JSON; ``--out PREFIX`` also writes ``PREFIX_statistics.json``
+as compare_phase.py:220-227 does.  Formats (``--fmt1``/``--fmt2``; default
+``auto``: .npy by extension, else by file size, complex128 or complex64):
+
+* ``complex128``: interleaved float64 pairs, column-major (``SlcMatr_complex.dat``);
+* ``interleaved`` / ``interleaved_f32``: interleaved float32 pairs,
+  column-major (``SlcPx_*_InterleavedF32.dat``, sar_focuser_puntual_noui.py:455-466;
+  compare_phase.py:8-21);
+* ``split`` / ``split_f32``: all real parts then all imaginary parts, float32,
+  column-major (``SlcPx_*_SplitF32.dat``, sar_focuser_puntual_noui.py:441-452;
+  compare_phase.py:22-29);
+* ``truth``: complex64, column-major (compare_phase.py:33-37; the same bytes
+  as ``interleaved``);
+* ``slcmatr``: the ``SlcMatr_real.dat`` / ``SlcMatr_imag.dat`` float64 pair
+  (README's outputs): give either file or their directory;
+* ``npy``: a NumPy complex array (``SlcPx_*.npy``).
 """
 from __future__ import annotations
 
 import argparse
 import json
+import os
 
 import numpy as np
 
@@ -45,12 +63,18 @@ def coherence(a, b) -> float:
     return float(np.abs(np.sum(a * np.conj(b))) / den) if den > 0 else 1.0
 
 
-def phase_stats(a, b, rel_threshold: float = 1e-5) -> dict:
-    """Wrapped phase-difference statistics (radians) of a against b."""
+def phase_stats(a, b, rel_threshold: float | None = 1e-5) -> dict:
+    """Wrapped phase-difference statistics (radians) of a against b.
+
+    ``rel_threshold`` None keeps every pixel (the reference tool's
+    ``--no-mask``)."""
     a, b = _np(a), _np(b)
-    amax = max(np.abs(b).max(initial=0.0), np.abs(a).max(initial=0.0))
-    thr = rel_threshold * amax
-    m = (np.abs(a) > thr) & (np.abs(b) > thr)
+    if rel_threshold is None:
+        m = np.ones(a.shape, dtype=bool)
+    else:
+        amax = max(np.abs(b).max(initial=0.0), np.abs(a).max(initial=0.0))
+        thr = rel_threshold * amax
+        m = (np.abs(a) > thr) & (np.abs(b) > thr)
     d = np.angle(a[m] * np.conj(b[m]))
     if d.size == 0:
         return {"valid_pixels": 0}
@@ -72,31 +96,95 @@ def phase_stats(a, b, rel_threshold: float = 1e-5) -> dict:
     }
 
 
-def compare(a, b) -> dict:
+def compare(a, b, rel_threshold: float | None = 1e-5) -> dict:
     """rel-L2, coherence and RMS phase error (mrad) of a against reference b."""
-    ps = phase_stats(a, b)
+    ps = phase_stats(a, b, rel_threshold)
     return {"rel_l2": rel_l2(a, b), "coherence": coherence(a, b),
             "rms_phase_mrad": ps.get("rms_mrad", 0.0), "phase": ps}
 
 
-def load_image(path: str, shape: tuple[int, int]) -> np.ndarray:
-    if path.endswith(".npy"):
-        return np.load(path).reshape(shape, order="F")
-    flat = np.fromfile(path, dtype=np.complex128)
-    if flat.size != shape[0] * shape[1]:
-        raise ValueError(f"{path}: {flat.size} complex128 values, expected {shape[0] * shape[1]}")
-    return flat.reshape(shape, order="F")
+FORMATS = ("auto", "complex128", "interleaved", "interleaved_f32", "split", "split_f32", "truth",
+           "slcmatr", "npy")
+
+
+def _slcmatr_paths(path: str) -> tuple[str, str]:
+    if os.path.isdir(path):
+        return (os.path.join(path, "SlcMatr_real.dat"), os.path.join(path, "SlcMatr_imag.dat"))
+    d, name = os.path.split(path)
+    if "SlcMatr_real" in name:
+        return path, os.path.join(d, name.replace("SlcMatr_real", "SlcMatr_imag"))
+    if "SlcMatr_imag" in name:
+        return os.path.join(d, name.replace("SlcMatr_imag", "SlcMatr_real")), path
+    raise ValueError(f"{path}: slcmatr wants SlcMatr_real.dat, SlcMatr_imag.dat or their "
+                     "directory")
+
+
+def load_image(path: str, shape: tuple[int, int], fmt: str = "auto") -> np.ndarray:
+    """A complex image of ``shape`` (column-major on disk) in format ``fmt``."""
+    from .datfiles import read_dat, read_slc
+
+    if fmt not in FORMATS:
+        raise ValueError(f"unknown image format {fmt!r}; one of {FORMATS}")
+    n = shape[0] * shape[1]
+    if fmt == "auto":
+        if path.endswith(".npy"):
+            fmt = "npy"
+        else:
+            size = os.path.getsize(path)
+            if size == 16 * n:
+                fmt = "complex128"
+            elif size == 8 * n:
+                fmt = "interleaved"
+            else:
+                raise ValueError(f"{path}: {size} bytes is neither complex128 nor complex64 for "
+                                 f"shape {tuple(shape)}; name the format")
+    if fmt == "npy":
+        a = np.load(path)
+        if a.size != n:
+            raise ValueError(f"{path}: {a.size} values, expected {n}")
+        return a.reshape(shape, order="F") if a.shape != tuple(shape) else a
+    if fmt == "slcmatr":
+        re, im = _slcmatr_paths(path)
+        return read_dat(re, np.float64, shape) + 1j * read_dat(im, np.float64, shape)
+    key = {"complex128": "complex", "interleaved": "interleaved_f32", "truth": "interleaved_f32",
+           "split": "split_f32"}.get(fmt, fmt)
+    return read_slc(path, shape, key)
+
+
+def _shape(tokens) -> tuple[int, int]:
+    vals = [int(v) for t in tokens for v in str(t).replace(",", " ").split()]
+    if len(vals) != 2:
+        raise ValueError(f"--shape wants two sizes, got {tokens}")
+    return vals[0], vals[1]
 
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    ap.add_argument("image")
-    ap.add_argument("reference")
-    ap.add_argument("--shape", type=int, nargs=2, required=True)
+    ap.add_argument("image", nargs="?")
+    ap.add_argument("reference", nargs="?")
+    ap.add_argument("--file1", help="image (the reference tool's spelling)")
+    ap.add_argument("--file2", help="reference image (the reference tool's spelling)")
+    ap.add_argument("--shape", nargs="+", required=True, help="D0 D1 or D0,D1")
+    ap.add_argument("--fmt1", default="auto", choices=FORMATS)
+    ap.add_argument("--fmt2", default="auto", choices=FORMATS)
+    ap.add_argument("--no-mask", action="store_true",
+                    help="phase statistics over every pixel (no amplitude threshold)")
+    ap.add_argument("--out", default=None, help="also write OUT_statistics.json")
     ns = ap.parse_args(argv)
-    a = load_image(ns.image, tuple(ns.shape))
-    b = load_image(ns.reference, tuple(ns.shape))
-    print(json.dumps(compare(a, b), indent=2))
+    f1 = ns.file1 or ns.image
+    f2 = ns.file2 or ns.reference
+    if not f1 or not f2:
+        ap.error("two images are needed (positional or --file1/--file2)")
+    shape = _shape(ns.shape)
+    a = load_image(f1, shape, ns.fmt1)
+    b = load_image(f2, shape, ns.fmt2)
+    stats = compare(a, b, None if ns.no_mask else 1e-5)
+    text = json.dumps(stats, indent=2)
+    print(text)
+    if ns.out:
+        with open(f"{ns.out}_statistics.json", "w") as f:
+            f.write(text + "\n")
+    return stats
 
 
 if __name__ == "__main__":

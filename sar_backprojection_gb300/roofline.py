@@ -15,8 +15,11 @@ not a tensor contraction.  Algorithmic operations per pixel-pulse:
 
 Kahan compensation and range-bin tie re-derivation are not counted.
 Peak pixel-pulses/s = min(FP32 FMA lanes/s / N_FP32, SFU ops/s / N_SFU) for
-the mixed kernel and FP64 FMA lanes/s / N_FP64 for the FP64 kernel, with the
-lane rates measured on the device by libsarbp's probe kernels.
+the mixed kernel and FP64 FMA lanes/s / N_FP64 for the FP64 kernel.  The
+rates are the larger of two figures: the device's nominal rate (SMs x 128
+FP32 lanes, x 16 SFU lanes per clock at the maximum SM clock; GB300's
+nominal 1.25 TFLOP/s FP64) and the rate libsarbp's probe kernels measure on
+the device, so a fraction never flatters a kernel by a probe that ran slow.
 
 Algorithmic bytes per scene (for the HBM view): the raw-data rows inside the
 scene's aperture hull read once (8 B per range bin per pulse), 29 B per DEM
@@ -32,6 +35,18 @@ DEM_BYTES_PER_PIXEL = 8 * 3 + 4 + 4 + 1
 TRAJ_BYTES_PER_PULSE = 24
 OUT_BYTES_PER_PIXEL = 16
 RAW_BYTES_PER_SAMPLE = 8
+
+
+FP32_LANES_PER_SM_CLK = 128
+SFU_LANES_PER_SM_CLK = 16
+FP64_FMA_LANES_NOMINAL = 1.25e12 / 2      # GB300: 1.25 TFLOP/s FP64, 2 flops per FMA
+
+
+def nominal_rates(sms: int, sm_max_mhz: float) -> tuple[float, float, float]:
+    """(FP32 FMA lanes/s, SFU ops/s, FP64 FMA lanes/s) of the device on paper."""
+    clk = sm_max_mhz * 1e6
+    return (sms * FP32_LANES_PER_SM_CLK * clk, sms * SFU_LANES_PER_SM_CLK * clk,
+            FP64_FMA_LANES_NOMINAL)
 
 
 def peak_pixel_pulses(ffma_lanes_per_s: float, sfu_per_s: float) -> float:

@@ -289,9 +289,12 @@ def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
         size = int(np.prod(tuple(a.shape)))
         if size != npix:
             raise ValueError(f"{name} has {size} elements, the DEM grid has {npix}")
+    # the reference reads the trajectory only at pulses 0 < a < Naz-1
+    # (sar_focuser_puntual_noui.py:46-55, :71-73): Naz-1 points suffice
     for name, w in (("wgsx", wgsx), ("wgsy", wgsy), ("wgsz", wgsz)):
-        if int(np.prod(tuple(w.shape))) < naz:
-            raise ValueError(f"{name} is shorter than Raw_Data's {naz} pulses")
+        if int(np.prod(tuple(w.shape))) < naz - 1:
+            raise ValueError(f"{name} has fewer than the {naz - 1} points Raw_Data's {naz} "
+                             "pulses need")
 
     if not torch.cuda.is_available():
         raise RuntimeError("sar_backprojection_gb300 needs a CUDA device (no CPU fallback)")
@@ -310,6 +313,11 @@ def scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
 
     def traj(w):
         t = _as_tensor(_cast_host(w, np.float64)).reshape(-1)
+        if t.numel() < naz:
+            # pulse Naz-1 never contributes; the mixed path's per-pulse tables
+            # still span every pulse, so repeat the last point for it
+            pad = (t[-1:] if t.numel() else torch.zeros(1, dtype=t.dtype)).expand(naz - t.numel())
+            t = torch.cat([t, pad])
         return _to_device(t, device, sm).contiguous()
 
     scene = DeviceScene(

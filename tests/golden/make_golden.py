@@ -1,8 +1,8 @@
 """Generate the golden fixtures in this directory from the reference itself.
 
 Runs the UNMODIFIED reference focusing call ``FocalizzatoreBpPx`` from
-``sar_focuser_puntual_noui.py`` (read from the reference checkout, default
-/root/reference, or $SARBP_REFERENCE_DIR) under plain NumPy: numba is not
+``sar_focuser_puntual_noui.py`` (read from the reference checkout named by
+``--reference DIR`` or, failing that, $SARBP_REFERENCE_DIR) under plain NumPy: numba is not
 installed, so a stub module whose ``jit`` returns the function unchanged and
 whose ``prange`` is ``range`` is placed in ``sys.modules`` first.  NumPy and
 Numba's nopython mode agree on the operations used (IEEE arithmetic, sqrt,
@@ -24,7 +24,7 @@ Fixtures written (all .npz):
                        the host it ran on: the reference's own CPU speed,
                        which cannot be measured where the reference is absent.
 
-Usage: python tests/golden/make_golden.py [--only small|edges|ties|timing]
+Usage: python tests/golden/make_golden.py --reference DIR [--only small|edges|ties|timing]
 """
 from __future__ import annotations
 
@@ -49,9 +49,12 @@ sys.path.insert(0, str(ROOT))
 from sar_backprojection_gb300 import synth  # noqa: E402
 
 
-def load_reference():
+def load_reference(ref_dir: str | None):
     """Import the reference module with a numba stub (no files written)."""
-    ref_dir = Path(os.environ.get("SARBP_REFERENCE_DIR", "/root/reference"))
+    ref_dir = ref_dir or os.environ.get("SARBP_REFERENCE_DIR")
+    if not ref_dir:
+        raise SystemExit("name the reference checkout: --reference DIR or $SARBP_REFERENCE_DIR")
+    ref_dir = Path(ref_dir)
     src = ref_dir / "sar_focuser_puntual_noui.py"
     if not src.exists():
         raise FileNotFoundError(f"reference source not found: {src}")
@@ -164,7 +167,8 @@ INPUT_KEYS = ("xxg1", "yyg1", "zzg1", "Mask", "Index", "Sint", "wgsx", "wgsy", "
 
 def main(argv):
     only = argv[argv.index("--only") + 1] if "--only" in argv else None
-    mod = load_reference()
+    ref = argv[argv.index("--reference") + 1] if "--reference" in argv else None
+    mod = load_reference(ref)
     if only in (None, "small", "timing"):
         spec = synth.config_small()
         scene = synth.generate(spec)

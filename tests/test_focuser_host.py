@@ -34,6 +34,18 @@ def test_size_mismatch_and_short_trajectory():
     a[5] = a[5][:100]
     with pytest.raises(ValueError, match="wgsx"):
         FocalizzatoreBpPx(*a)
+    # the reference reads pulses 0 < a < Naz-1 only: Naz-1 points are enough,
+    # Naz-2 are not
+    naz = a[8].shape[1]
+    a = _args()
+    a[6] = a[6][:naz - 2]
+    with pytest.raises(ValueError, match="wgsy"):
+        FocalizzatoreBpPx(*a)
+    a = _args()
+    a[5], a[6], a[7] = a[5][:naz - 1], a[6][:naz - 1], a[7][:naz - 1]
+    if not torch.cuda.is_available():
+        with pytest.raises(RuntimeError, match="CUDA"):   # past the argument checks
+            FocalizzatoreBpPx(*a)
 
 
 def test_batched_rejects_bad_batch_size():

@@ -62,3 +62,29 @@ def test_autotuner_picks_a_candidate(scenes):
     assert (t.tile0, t.tile1, t.window, t.chunk) in batch.STAGED_TILINGS and t.staged == 1
     assert at.pick(scenes[:3]).tile0 == t.tile0        # cached
     assert len(at.timings) == 1
+
+
+def test_uneven_48_scene_batch():
+    """The batch the bench times: the 48 uneven scenes (DEM 128x32..2000x250,
+    2001..20001 pulses, Sint 200..1800), the tiling the autotuner picks for
+    them, one graph-captured persistent launch without checksum outputs.
+    Every scene's image must equal its single-scene launch of the same tuning
+    bit for bit and meet the mixed-precision bars against the FP64 kernel
+    (whose range bins and values are pinned to the oracle elsewhere)."""
+    specs = synth.uneven_specs(48)
+    scenes = [scene_to_device(*synth.focus_args(synth.generate(sp, raw_device="cuda")),
+                              device="cuda") for sp in specs]
+    tuning = batch.Autotuner(repeats=1).pick(scenes)
+    bf = batch.BatchFocuser(scenes, tuning, graph=True)
+    for _ in range(2):
+        bf.run()
+    torch.cuda.synchronize()
+    for sl, img in zip(bf.slots, bf.images()):
+        single = focus(sl.scene, "mixed", tuning=tuning).check()
+        torch.cuda.synchronize()
+        assert torch.equal(sl.out, single.image)
+        ref = focus(sl.scene, "fp64")
+        torch.cuda.synchronize()
+        q = quality.compare(torch.view_as_real(img.t().reshape(-1)).cpu().numpy(),
+                            ref.image.cpu().numpy())
+        assert q["coherence"] >= 0.9999 and q["rms_phase_mrad"] <= 1.0 and q["rel_l2"] <= 1e-3, q

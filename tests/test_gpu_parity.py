@@ -193,3 +193,89 @@ def test_tile_queue_matches_one_cta_per_tile(full_scene, tiling):
     for x, y in zip(a[:3], b[:3]):
         assert np.array_equal(x, y)
     assert np.array_equal(a[3][:3], b[3][:3]) and b[3][3] == 0
+
+
+def image_of(image: torch.Tensor, shape) -> np.ndarray:
+    """complex128 (dim0, dim1) host image of a device (npix, 2) float64 image."""
+    flat = image.cpu().numpy().view(np.complex128).reshape(-1)
+    return np.reshape(flat, shape, order="F")
+
+
+def _bench_tunings():
+    """The staged candidates bench.py times on the full workload (it measures
+    the first within 1 % of the fastest)."""
+    import bench
+    return [dict(zip(bench.TUNING_FIELDS, c)) for c in bench.AUTOTUNE_CANDIDATES]
+
+
+@pytest.mark.parametrize("tuning", _bench_tunings(),
+                         ids=lambda t: f"c{t['chunk']}_{t['tile0']}x{t['tile1']}w{t['window']}")
+def test_full_workload_production_launch(full_scene, full_oracle, tuning):
+    """The launch bench.py times: no checksum output (the production kernel
+    instantiation), each of the bench's candidate tunings, on the full
+    workload.  Its image must equal the diagnostic launch's bit for bit, the
+    diagnostic launch's range bins must equal the oracle's, and the image must
+    meet the mixed-precision bars against the oracle's image."""
+    oimg, onv, ocs = full_oracle
+    ds = scene_to_device(*synth.focus_args(full_scene))
+    prod = focus(ds, "mixed", tuning=tuning).check()
+    prod_img = prod.image.clone()
+    diag = focus(ds, "mixed", tuning=tuning, diagnostics=True).check()
+    torch.cuda.synchronize()
+    assert torch.equal(prod_img, diag.image)
+    shape = (ds.dim0, ds.dim1)
+    nv = diag.nvalid.cpu().numpy().reshape(shape, order="F")
+    cs = diag.checksum.cpu().numpy().view(np.uint64).reshape(shape, order="F")
+    assert np.array_equal(nv, onv) and np.array_equal(cs, ocs)
+    assert int(diag.counters[3].item()) == 0
+    img = image_of(prod_img, shape)
+    q = assert_mixed_quality(img, oimg)
+    print("production launch", tuning, {k: q[k] for k in ("rel_l2", "coherence",
+                                                          "rms_phase_mrad")})
+
+
+def test_full_workload_streamed_drop_in(full_scene, full_oracle):
+    """The drop-in call as the bench's e2e measures it: host inputs in the
+    reference's layout, precision="mixed" with the bench's preferred tuning,
+    the reachable range bins streamed up in pulse blocks while focusing runs.
+    The returned image must equal the resident launch of the same tuning bit
+    for bit (whose range bins equal the oracle's) and meet the bars against
+    the oracle."""
+    from sar_backprojection_gb300 import FocalizzatoreBpPx, focuser
+
+    oimg, onv, ocs = full_oracle
+    tuning = _bench_tunings()[0]
+    host = dict(full_scene)
+    host["RawData"] = full_scene["RawData"].cpu()       # (nra, naz), pulse-major memory
+    img = FocalizzatoreBpPx(*synth.focus_args(host), precision="mixed", tuning=tuning)
+    assert focuser.last_call["streamed"]
+    assert img.shape == (4000, 250) and img.dtype == np.complex128
+    ds = scene_to_device(*synth.focus_args(full_scene))
+    diag = focus(ds, "mixed", tuning=tuning, diagnostics=True).check()
+    torch.cuda.synchronize()
+    shape = (ds.dim0, ds.dim1)
+    assert np.array_equal(img, image_of(diag.image, shape))
+    nv = diag.nvalid.cpu().numpy().reshape(shape, order="F")
+    cs = diag.checksum.cpu().numpy().view(np.uint64).reshape(shape, order="F")
+    assert np.array_equal(nv, onv) and np.array_equal(cs, ocs)
+    assert_mixed_quality(img, oimg)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_trajectory_of_naz_minus_one_points(precision):
+    """The reference reads the trajectory only at pulses 0 < a < Naz-1, so it
+    accepts Naz-1 points (sar_focuser_puntual_noui.py:46-55): on the edge-case
+    scene (apertures at pulses 0, 1, Naz-2, Naz-1) a trajectory one point
+    short gives the oracle's range bins and the same image bits as the full
+    one."""
+    scene, ref = load_golden_scene("edges")
+    naz = scene["RawData"].shape[1]
+    short = dict(scene)
+    for k in ("wgsx", "wgsy", "wgsz"):
+        short[k] = np.ascontiguousarray(scene[k][: naz - 1])
+    full = run(scene, precision)
+    cut = run(short, precision)
+    for x, y in zip(full[:3], cut[:3]):
+        assert np.array_equal(x, y)
+    _, onv, ocs = oracle.focus_scene(short)
+    assert np.array_equal(cut[1], onv) and np.array_equal(cut[2], ocs)

@@ -4,18 +4,21 @@ sarbp_focus_mixed_noalloc serves callers that cannot allocate device memory
 (plugins in applications that own the device's memory pool, real-time
 pipelines that may not call cudaMalloc, bindings without an allocator): its
 scratch is a library-owned device array instead of a caller workspace.  Its
-results must equal the workspace entry point's, on two calls in a row (the
-array keeps the previous call's contents), within this suite's tolerances:
-range-bin counts and checksums bit-exact, mixed-precision image quality bars.
-This file is collected last so that a failure here never hides another test.
+results must equal the workspace entry point's under the same tuning, bit
+for bit (image, range-bin counts and checksums), on two calls in a row (the
+array keeps the previous call's contents), with one CTA per tile and with
+the persistent tile queue.  A bounded device wait that gives up must come
+back from the call itself as SARBP_ETIMEOUT, since its caller holds no
+workspace whose status it could read.  This file is collected last so that
+a failure here never hides another test.
 """
 import ctypes as C
 
-import numpy as np
 import pytest
 import torch
 
-from sar_backprojection_gb300 import _lib, focus, quality, scene_to_device, synth
+from sar_backprojection_gb300 import _lib, focus, scene_to_device, synth
+from sar_backprojection_gb300.focuser import resolve_tuning
 
 pytestmark = pytest.mark.gpu
 
@@ -26,32 +29,59 @@ def _scene(seed):
     return scene_to_device(*synth.focus_args(synth.generate(spec)), device="cuda:0")
 
 
-def _noalloc(ds):
+def _noalloc(ds, tuning=None):
     lib = _lib.load()
     out = torch.empty((ds.npix, 2), dtype=torch.float64, device=ds.device)
     nv = torch.empty(ds.npix, dtype=torch.int32, device=ds.device)
     cs = torch.empty(ds.npix, dtype=torch.int64, device=ds.device)
-    rc = lib.sarbp_focus_mixed_noalloc(C.byref(ds.struct()), None, out.data_ptr(),
-                                       nv.data_ptr(), cs.data_ptr(), None,
+    ctr = torch.zeros(_lib.NUM_COUNTERS, dtype=torch.int64, device=ds.device)
+    t = C.byref(resolve_tuning(tuning)) if tuning is not None else None
+    rc = lib.sarbp_focus_mixed_noalloc(C.byref(ds.struct()), t, out.data_ptr(),
+                                       nv.data_ptr(), cs.data_ptr(), ctr.data_ptr(),
                                        torch.cuda.current_stream(ds.device).cuda_stream)
-    _lib.check(rc)
     torch.cuda.synchronize(ds.device)
-    return out, nv, cs
+    return rc, out, nv, cs, ctr
 
 
-def test_noalloc_matches_workspace_entry_point_twice():
+@pytest.mark.parametrize("tuning", [None, dict(chunk=32, tile0=16, tile1=8, staged=2,
+                                               window=128)],
+                         ids=["default", "queue"])
+def test_noalloc_matches_workspace_entry_point_twice(tuning):
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     torch.cuda.set_device(0)
     for seed in (21, 22):                     # two calls in a row, different scenes
         ds = _scene(seed)
-        ref = focus(ds, "mixed", diagnostics=True)
+        ref = focus(ds, "mixed", tuning=tuning, diagnostics=True).check()
         torch.cuda.synchronize()
-        out, nv, cs = _noalloc(ds)
+        rc, out, nv, cs, ctr = _noalloc(ds, tuning)
+        _lib.check(rc)
+        assert torch.equal(out, ref.image)
         assert torch.equal(nv, ref.nvalid)
         assert torch.equal(cs, ref.checksum)
-        q = quality.compare(out.cpu().numpy(), ref.image.cpu().numpy())
-        assert q["coherence"] >= 0.9999 and q["rms_phase_mrad"] <= 1.0 and q["rel_l2"] <= 1e-3, q
+        assert int(ctr[_lib.CTR_TIMEOUTS].item()) == 0
+
+
+def test_noalloc_reports_a_wait_that_runs_out():
+    """withhold=1 leaves one stage copy of every pass unissued, so its bounded
+    wait gives up: the call returns SARBP_ETIMEOUT, and the next call on the
+    same context is bit-identical to the workspace entry point again."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.set_device(0)
+    ds = _scene(24)
+    bad = dict(chunk=64, tile0=16, tile1=16, staged=1, window=160, wait_polls=64, withhold=1)
+    rc, _, _, _, ctr = _noalloc(ds, bad)
+    assert rc == _lib.SARBP_ETIMEOUT
+    assert "gave up" in _lib.last_error()
+    assert int(ctr[_lib.CTR_TIMEOUTS].item()) > 0
+    good = dict(bad, withhold=0, wait_polls=0)
+    rc, out, nv, _, ctr = _noalloc(ds, good)
+    _lib.check(rc)
+    ref = focus(ds, "mixed", tuning=good, diagnostics=True).check()
+    torch.cuda.synchronize()
+    assert torch.equal(out, ref.image) and torch.equal(nv, ref.nvalid)
+    assert int(ctr[_lib.CTR_TIMEOUTS].item()) == 0
 
 
 def test_noalloc_rejects_scenes_beyond_its_limit():
