@@ -184,9 +184,7 @@ def save_scene(data_dir, scene: dict) -> dict:
     d.mkdir(parents=True, exist_ok=True)
     dim0, dim1 = np.shape(scene["xxg1"])
     raw = scene["RawData"]
-    if hasattr(raw, "detach"):
-        raw = raw.detach().cpu().numpy()
-    nra, naz = raw.shape
+    nra, naz = (int(v) for v in raw.shape)
     names = scene_filenames(dim0, dim1, nra, naz)
     for k in DEM_NAMES:
         write_dat(d / names[k], scene[k], np.float64)
@@ -194,7 +192,17 @@ def save_scene(data_dir, scene: dict) -> dict:
         write_dat(d / names[k], scene[k], dt)
     for k in TRAJ_NAMES:
         write_dat(d / names[k], scene[k], np.float64)
-    write_dat(d / names["RawData"], raw, np.complex64)
+    if hasattr(raw, "detach"):
+        # a (Nra, Naz) tensor: the file's column-major bytes are its pulse
+        # rows, written in blocks of rows (no whole host copy)
+        rows = raw.detach().t()
+        with open(d / names["RawData"], "wb") as f:
+            step = max(1, (256 << 20) // max(1, 8 * nra))
+            for a0 in range(0, naz, step):
+                blk = rows[a0:a0 + step].to("cpu").contiguous()
+                blk.numpy().astype(np.complex64, copy=False).tofile(f)
+    else:
+        write_dat(d / names["RawData"], raw, np.complex64)
     for k in SCALAR_NAMES:
         write_dat(d / names[k], np.array([scene[k]], dtype=np.float64))
     return names

@@ -96,6 +96,22 @@ def scaled_full(seed: int, dim0: int, dim1: int, naz: int, sint_lo: int, sint_hi
                    n_targets=max(8, int(200 * dim0 * dim1 / 1.0e6)))
 
 
+def large_spec(seed: int = 6, dim_az: int = 32000, dim_rg: int = 4000, naz: int = 403484,
+               n_targets: int = 2000) -> SceneSpec:
+    """The reference's large-scene size (DEM 4000 x 32000, RawData 4762 x
+    403484 = 15.4 GB; main_gpu.py:321-324) with config_full's physics.
+
+    Azimuth is the first axis of the generated grid (``azimuth_columns``
+    turns it into the reference's (DimRg, DimAz) layout): dim_az pixels over
+    the whole track, dim_rg range pixels at 0.7 m ground spacing (slant
+    ranges 3.6-5.8 km inside the 4762-bin swath)."""
+    track = 0.5 * (naz - 1)
+    az = track / dim_az
+    return replace(config_full(seed), name=f"large_{dim_rg}x{dim_az}_{naz}", dim0=dim_az,
+                   dim1=dim_rg, az_spacing=az, x0=0.5 * az, rg_spacing=0.7, naz=naz,
+                   n_targets=n_targets)
+
+
 def uneven_specs(n: int = 48, seed: int = 4) -> list[SceneSpec]:
     """Scenes with log-uniform sizes: DEM 128x32..2000x250, 2001..20001 pulses,
     Sint 200..1800."""

@@ -29,6 +29,19 @@ def test_scene_round_trip(tmp_path, tiny_scene):
     assert raw[1] == tiny_scene["Sint"][1, 0]
 
 
+def test_scene_round_trip_from_a_tensor(tmp_path, tiny_scene):
+    """Raw data held as a (Nra, Naz) tensor view of pulse-major storage (the
+    GPU generator's form) is written in pulse-row blocks: same file bytes."""
+    import torch
+    sc = dict(tiny_scene)
+    rows = torch.from_numpy(np.ascontiguousarray(np.asarray(tiny_scene["RawData"]).T))
+    sc["RawData"] = rows.t()
+    names = datfiles.save_scene(tmp_path / "t", sc)
+    datfiles.save_scene(tmp_path / "n", tiny_scene)
+    a = (tmp_path / "t" / names["RawData"]).read_bytes()
+    assert a == (tmp_path / "n" / names["RawData"]).read_bytes()
+
+
 def test_raw_interleaved_layout(tmp_path):
     raw = (np.arange(12, dtype=np.float32) + 1j * -np.arange(12, dtype=np.float32))
     raw = np.asfortranarray(raw.reshape(3, 4, order="F").astype(np.complex64))
