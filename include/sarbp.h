@@ -359,6 +359,21 @@ SARBP_API int sarbp_queue_wait(sarbp_queue *queue, int64_t job);
 SARBP_API int sarbp_queue_destroy(sarbp_queue *queue);
 
 /*
+ * 8-bit amplitude preview of a focused image: out[i] = clip(|image[i]| *
+ * 255 / (scale_factor * mean|image|), 0, 255) truncated to uint8 -- the
+ * reference visualiser's scaling (img_visualizer.py:23-46, scale_factor 15)
+ * computed on the device.  image: npix complex128 (re, im) pairs; out: npix
+ * bytes (same pixel order); mean: optional (NULL), one double receiving
+ * mean|image|; scratch: device memory for the fixed-order partial sums (one
+ * double per block; SARBP_PREVIEW_SCRATCH_BYTES is enough on any GPU).  All
+ * pointers are device pointers.  Stream-ordered, no synchronisation.
+ */
+#define SARBP_PREVIEW_SCRATCH_BYTES 16384
+SARBP_API int sarbp_amplitude_u8(const double *image, int64_t npix, double scale_factor,
+                                 uint8_t *out, double *mean, double *scratch,
+                                 size_t scratch_bytes, void *stream);
+
+/*
  * Measurement helper (no counterpart in the reference, which publishes no
  * roofline): measures this device's issue rates with probe kernels on
  * `stream` and returns them in rates[0..3] = FP32 FMA lanes/s, SFU sin

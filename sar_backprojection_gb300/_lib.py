@@ -23,6 +23,7 @@ CTR_WINDOW_MISS = 1
 CTR_CHUNKS = 2
 CTR_TIMEOUTS = 3
 NUM_COUNTERS = 8
+PREVIEW_SCRATCH_BYTES = 16384
 
 
 class SarbpError(RuntimeError):
@@ -97,6 +98,7 @@ SIGNATURES = {
     "sarbp_copy_to_device_sm": (C.c_int, [_P, _P, C.c_int64, _P]),
     "sarbp_focus_mixed_noalloc": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, _P, _P,
                                             _P, _P]),
+    "sarbp_amplitude_u8": (C.c_int, [_P, C.c_int64, C.c_double, _P, _P, _P, C.c_size_t, _P]),
     "sarbp_tile_count": (C.c_int64, [C.POINTER(Scene), C.POINTER(Tuning)]),
     "sarbp_tile_costs": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, _P]),
     "sarbp_batch_workspace_size": (C.c_int64, [C.c_int32, C.c_int64]),

@@ -25,9 +25,15 @@
 // reach from the stage's pulses: per pixel, the distances to the stage's
 // first and last pulse positions (maximum) and to the chord between them
 // (minimum), widened by the stage's deviation from that chord and one bin on
-// each side; reduced over the tile in a prologue.  A bin outside the staged
-// window (a window wider than W) is read from global memory instead and
-// counted as a window miss, so correctness never depends on the window.
+// each side; reduced over the tile in a prologue.  When that interval is
+// wider than W bins, or reaches outside bins 0..nra-2, the stage runs on the
+// generic path, which tests every pulse's bin against the window and reads a
+// bin outside it from global memory (counted as a window miss).  Only when
+// the interval fits does a warp take the fast path, which reads the staged
+// window without a per-pulse test (a column outside it would be clamped to
+// the window's edge): its correctness rests on the prologue's bound being
+// conservative, which the margins above make it (tests compare the range
+// bins of rough-terrain scenes with the oracle's bit for bit).
 //
 // All mbarrier waits are bounded; a wait that gives up sets the CTA's stop
 // flag, every warp leaves the pass, and the CTA marks the workspace status

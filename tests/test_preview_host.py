@@ -1,23 +1,21 @@
-"""Amplitude preview: the reference visualiser's 15*mean scaling, PGM output."""
+"""Amplitude preview, host side: the PGM container and the no-fallback rule."""
 import numpy as np
+import pytest
+import torch
 
 from sar_backprojection_gb300 import preview
 
 
-def test_matches_reference_scaling(tmp_path):
-    rng = np.random.default_rng(0)
-    img = rng.standard_normal((40, 30)) + 1j * rng.standard_normal((40, 30))
-    img[3, 4] = 1000.0                                      # a bright target clips
-    u8 = preview.amplitude_u8(img, device="cpu").numpy()
-    mag = np.abs(img)
-    ref = np.clip(mag * (255.0 / (15 * np.mean(mag))), 0, 255).astype(np.uint8)
-    assert np.array_equal(u8, ref)
-    p = preview.write_pgm(tmp_path / "a.pgm", u8)
-    assert np.array_equal(preview.read_pgm(p), ref)
-    pairs = np.stack([img.real, img.imag], axis=-1)
-    assert np.array_equal(preview.amplitude_u8(pairs, device="cpu").numpy(), ref)
+def test_pgm_round_trip(tmp_path):
+    a = np.arange(40 * 30, dtype=np.uint8).reshape(40, 30)
+    p = preview.write_pgm(tmp_path / "a.pgm", a)
+    assert p.read_bytes().startswith(b"P5\n30 40\n255\n")
+    assert np.array_equal(preview.read_pgm(p), a)
+    with pytest.raises(ValueError):
+        preview.write_pgm(tmp_path / "b.pgm", a.reshape(-1))
 
 
-def test_all_zero_image():
-    u8 = preview.amplitude_u8(np.zeros((4, 5), dtype=np.complex128), device="cpu")
-    assert int(u8.max()) == 0
+@pytest.mark.skipif(torch.cuda.is_available(), reason="checks the no-GPU error")
+def test_no_cpu_fallback():
+    with pytest.raises(RuntimeError, match="CUDA"):
+        preview.amplitude_u8(np.ones((4, 5), dtype=np.complex128))
