@@ -381,9 +381,6 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                 tma_load_2d(base, raw_map, &sh.full_bar[b], window_start(q), (int)K);
                 bulk_load(base + Cfg::raw_bytes, ptab + K, (uint32_t)Cfg::tab_bytes,
                           &sh.full_bar[b]);
-                // the stage loaded NBUF stages from now: into L2 meanwhile
-                if (q + NBUF < npass)
-                    tma_prefetch_2d(raw_map, window_start(q + NBUF), (int)(K + NBUF * STAGE));
                 sh.last_parity[b] = use & 1;
                 sh.issued[b] = 1;
             };
@@ -465,7 +462,11 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                     // and read column 0 or a clamped column; nothing is added
                     const int colbias = S.n0 - b0 - 0x4B400000;
                     const float tie = 0.5f - S.eps;
-                    float sre = gre, sim = gim;
+                    // the stage's terms (vx + j*vy)*(wc - j*ws) as four sums:
+                    // (sre, sim) += v*wc and (bre, bim) += v*ws, one f32x2 FMA
+                    // each per pulse (the same per-lane sequence on every path);
+                    // re = sre + bim, im = sim - bre at the end of the stage
+                    float sre = gre, sim = gim, bre = 0.f, bim = 0.f;
                     uint32_t amb_mask = 0, miss_mask = 0, valid_mask;
                     // pulses of the stage inside this lane's aperture
                     const uint32_t apmask =
@@ -522,10 +523,17 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                                 float wc0, wc1, ws0, ws1;
                                 f2_unpack(f2_mul(w2, f2_pack(c0, c1)), wc0, wc1);
                                 f2_unpack(f2_mul(w2, f2_pack(s0, s1)), ws0, ws1);
-                                sre = fmaf(v0.x, wc0, fmaf(v0.y, ws0, sre));
-                                sim = fmaf(v0.y, wc0, fmaf(-v0.x, ws0, sim));
-                                sre = fmaf(v1.x, wc1, fmaf(v1.y, ws1, sre));
-                                sim = fmaf(v1.y, wc1, fmaf(-v1.x, ws1, sim));
+                                {
+                                    f2_t A2 = f2_pack(sre, sim), B2 = f2_pack(bre, bim);
+                                    const f2_t q0 = *reinterpret_cast<const f2_t *>(&v0);
+                                    const f2_t q1 = *reinterpret_cast<const f2_t *>(&v1);
+                                    A2 = f2_fma(q0, f2_dup(wc0), A2);
+                                    B2 = f2_fma(q0, f2_dup(ws0), B2);
+                                    A2 = f2_fma(q1, f2_dup(wc1), A2);
+                                    B2 = f2_fma(q1, f2_dup(ws1), B2);
+                                    f2_unpack(A2, sre, sim);
+                                    f2_unpack(B2, bre, bim);
+                                }
                                 if (kChecksum) {
                                     if ((apmask >> (2 * p)) & 1u) cs += mix64(K + 2 * p, col0 + b0);
                                     if ((apmask >> (2 * p + 1)) & 1u)
@@ -567,8 +575,10 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                             if (inap && amb) amb_mask |= 1u << j;
                             float wc, ws;
                             pulse_phasor(C, D, dR, P.beta_f, wc, ws);
-                            sre = fmaf(v.x, wc, fmaf(v.y, ws, sre));
-                            sim = fmaf(v.y, wc, fmaf(-v.x, ws, sim));
+                            sre = fmaf(v.x, wc, sre);
+                            sim = fmaf(v.y, wc, sim);
+                            bre = fmaf(v.x, ws, bre);
+                            bim = fmaf(v.y, ws, bim);
                             if (kChecksum && ok) cs += mix64(K + j, bin);
                         }
                     }
@@ -614,8 +624,10 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                             float wc, ws;
                             pulse_phasor(C, D, dR, P.beta_f, wc, ws);
                             const float dx = v_new.x - v_old.x, dy = v_new.y - v_old.y;
-                            sre = fmaf(dx, wc, fmaf(dy, ws, sre));
-                            sim = fmaf(dy, wc, fmaf(-dx, ws, sim));
+                            sre = fmaf(dx, wc, sre);
+                            sim = fmaf(dy, wc, sim);
+                            bre = fmaf(dx, ws, bre);
+                            bim = fmaf(dy, ws, bim);
                             valid_mask = ok_new ? (valid_mask | (1u << j)) : (valid_mask & ~(1u << j));
                             if (kChecksum) {
                                 if (ok_old) cs -= mix64(K + j, bin_old);
@@ -623,8 +635,8 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                             }
                         }
                         n += __popc(valid_mask);
-                        gre = sre;
-                        gim = sim;
+                        gre = sre + bim;
+                        gim = sim - bre;
                     }
                 }
                 // end of the chunk: rotate its partial by the reference phasor

@@ -74,16 +74,6 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const void *tensor_map, u
         : "memory");
 }
 
-// L2 prefetch of one box of a tiled tensor: no shared memory, no completion
-// to wait for (same x alignment rule as the load).
-__device__ __forceinline__ void tma_prefetch_2d(const void *tensor_map, int x, int y)
-{
-    asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"(
-                     reinterpret_cast<uint64_t>(tensor_map)),
-                 "r"(x), "r"(y)
-                 : "memory");
-}
-
 // 1-D bulk copy global -> shared (16-byte aligned addresses, size % 16 == 0).
 __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes,
                                           uint64_t *bar)
