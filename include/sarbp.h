@@ -359,6 +359,39 @@ SARBP_API int sarbp_queue_wait(sarbp_queue *queue, int64_t job);
 SARBP_API int sarbp_queue_destroy(sarbp_queue *queue);
 
 /*
+ * Host-memory jobs of the serving queue: the whole request path runs on the
+ * queue's worker thread, none of it on the caller's.
+ * sarbp_queue_reserve sets aside `bytes` of device memory (one allocation,
+ * made here, freed by sarbp_queue_destroy) from which each host job's
+ * device copies are carved -- DEM, masks, trajectory, raw rows, image and
+ * chunk tables, sarbp_queue_job_bytes(queue, scene) bytes; jobs are
+ * admitted in arrival order when a scene slot is free and their bytes fit.
+ * sarbp_queue_submit_host takes a scene whose array pointers are HOST
+ * pointers (same layouts as a device scene: column-major DEM grid arrays,
+ * raw data as rows of raw_pitch complex64 bins per pulse) and a host output
+ * of npix complex128; the worker uploads the small inputs, prepares the
+ * chunk tables, bounds the range bins the apertures can reach and uploads
+ * only those bins of each pulse row, runs the job's tiles in waves with
+ * the other jobs' and copies the image to `host_out` (bit-identical to
+ * sarbp_focus_mixed's).  Page-locked host memory (cudaHostAlloc, torch
+ * pin_memory) is read by SM loads and written asynchronously; pageable
+ * memory goes through the copy engine and holds the worker while it copies.
+ * The caller's buffers must stay valid until the job is reported done.
+ * sarbp_queue_completed drains up to `max` finished jobs (host or device)
+ * into ids[], with their completion time in seconds of the monotonic clock
+ * (CLOCK_MONOTONIC; Python's time.monotonic) in done_s[] and their status
+ * in status[] (both optional); it returns how many it reported.  A job is
+ * reported once, by whichever of sarbp_queue_completed / _poll / _wait sees
+ * it first.  No reference counterpart (the reference has no serving path).
+ */
+SARBP_API int sarbp_queue_reserve(sarbp_queue *queue, size_t bytes);
+SARBP_API int64_t sarbp_queue_job_bytes(sarbp_queue *queue, const sarbp_scene *scene);
+SARBP_API int64_t sarbp_queue_submit_host(sarbp_queue *queue, const sarbp_scene *host_scene,
+                                          double *host_out);
+SARBP_API int64_t sarbp_queue_completed(sarbp_queue *queue, int64_t *ids, double *done_s,
+                                        int32_t *status, int64_t max);
+
+/*
  * 8-bit amplitude preview of a focused image: out[i] = clip(|image[i]| *
  * 255 / (scale_factor * mean|image|), 0, 255) truncated to uint8 -- the
  * reference visualiser's scaling (img_visualizer.py:23-46, scale_factor 15)

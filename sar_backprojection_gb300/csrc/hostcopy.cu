@@ -90,6 +90,66 @@ static int copy_grid(int64_t work_units)
     return (int)(work_units < g ? (work_units > 0 ? work_units : 1) : g);
 }
 
+static void launch_copy_bytes(void *dst, const void *sv, int64_t bytes, cudaStream_t stream)
+{
+    const uintptr_t sa = reinterpret_cast<uintptr_t>(sv), da = reinterpret_cast<uintptr_t>(dst);
+    int64_t head = bytes, nvec = 0;               // all bytes one by one ...
+    if ((sa & 15) == (da & 15)) {                 // ... unless the ends align alike
+        head = (int64_t)((16 - (sa & 15)) & 15);
+        if (head > bytes) head = bytes;
+        nvec = (bytes - head) / 16;
+    }
+    // CTAs for the 16-byte words and for the bytes copied one by one (all of
+    // them when the ends are not aligned alike), 16 per thread
+    const int64_t singles = bytes - nvec * 16;
+    const int64_t units = (nvec + kCopyThreads - 1) / kCopyThreads +
+                          (singles + 16 * kCopyThreads - 1) / (16 * kCopyThreads);
+    copy_bytes_kernel<<<copy_grid(units), kCopyThreads, 0, stream>>>(
+        static_cast<unsigned char *>(dst), static_cast<const unsigned char *>(sv), bytes, head,
+        nvec);
+}
+
+int h2d_bytes(void *dst, const void *src, int64_t bytes, cudaStream_t stream)
+{
+    if (bytes <= 0) return SARBP_OK;
+    if (const void *sv = device_view(src)) {
+        launch_copy_bytes(dst, sv, bytes, stream);
+        return cuda_status(cudaGetLastError(), "host copy (SM loads)");
+    }
+    return cuda_status(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyHostToDevice, stream),
+                       "host copy");
+}
+
+int d2h_bytes(void *dst, const void *src, int64_t bytes, cudaStream_t stream)
+{
+    if (bytes <= 0) return SARBP_OK;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, dst) == cudaSuccess && at.type == cudaMemoryTypeHost &&
+        at.devicePointer) {
+        launch_copy_bytes(at.devicePointer, src, bytes, stream);
+        return cuda_status(cudaGetLastError(), "device-to-host copy (SM stores)");
+    }
+    cudaGetLastError();
+    return cuda_status(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDeviceToHost, stream),
+                       "device-to-host copy");
+}
+
+int h2d_rows(float2 *dst, int64_t dpitch, const float2 *src, int64_t spitch, int64_t lo,
+             int64_t n, int64_t rows, cudaStream_t stream)
+{
+    if (n <= 0 || rows <= 0) return SARBP_OK;
+    if (const void *sv = device_view(src)) {
+        gather_rows_kernel<<<copy_grid(rows), kCopyThreads, 0, stream>>>(
+            dst, dpitch, static_cast<const float2 *>(sv), spitch, lo, n, rows);
+        return cuda_status(cudaGetLastError(), "raw rows copy (SM loads)");
+    }
+    return cuda_status(cudaMemcpy2DAsync(dst + lo, (size_t)dpitch * sizeof(float2), src + lo,
+                                         (size_t)spitch * sizeof(float2),
+                                         (size_t)n * sizeof(float2), (size_t)rows,
+                                         cudaMemcpyHostToDevice, stream),
+                       "raw rows copy");
+}
+
 }  // namespace sarbp
 
 using namespace sarbp;
@@ -133,20 +193,6 @@ extern "C" SARBP_API int sarbp_copy_to_device_sm(void *dst, const void *src, int
                   "into the device's address space (or device memory)");
         return SARBP_EINVAL;
     }
-    const uintptr_t sa = reinterpret_cast<uintptr_t>(sv), da = reinterpret_cast<uintptr_t>(dst);
-    int64_t head = bytes, nvec = 0;               // all bytes one by one ...
-    if ((sa & 15) == (da & 15)) {                 // ... unless the ends align alike
-        head = (int64_t)((16 - (sa & 15)) & 15);
-        if (head > bytes) head = bytes;
-        nvec = (bytes - head) / 16;
-    }
-    // CTAs for the 16-byte words and for the bytes copied one by one (all of
-    // them when the ends are not aligned alike), 16 per thread
-    const int64_t singles = bytes - nvec * 16;
-    const int64_t units = (nvec + kCopyThreads - 1) / kCopyThreads +
-                          (singles + 16 * kCopyThreads - 1) / (16 * kCopyThreads);
-    copy_bytes_kernel<<<copy_grid(units), kCopyThreads, 0, static_cast<cudaStream_t>(stream)>>>(
-        static_cast<unsigned char *>(dst), static_cast<const unsigned char *>(sv), bytes, head,
-        nvec);
+    launch_copy_bytes(dst, sv, bytes, static_cast<cudaStream_t>(stream));
     return cuda_status(cudaGetLastError(), "sarbp_copy_to_device_sm launch");
 }

@@ -197,4 +197,12 @@ int tile_order(const SceneParams &P, const sarbp_tuning &T, const MixedLayout &L
                cudaStream_t stream);
 size_t tile_sort_bytes(int64_t ntiles);
 int tile_count(const SceneParams &P, const sarbp_tuning &T, int64_t *nt);
+
+// host -> device copies (hostcopy.cu): SM loads when the source is mapped
+// page-locked host memory (or device memory), the copy engine otherwise
+int h2d_bytes(void *dst, const void *src, int64_t bytes, cudaStream_t stream);
+// device -> host: SM stores into mapped page-locked memory, else the copy engine
+int d2h_bytes(void *dst, const void *src, int64_t bytes, cudaStream_t stream);
+int h2d_rows(float2 *dst, int64_t dpitch, const float2 *src, int64_t spitch, int64_t lo,
+             int64_t n, int64_t rows, cudaStream_t stream);
 }  // namespace sarbp

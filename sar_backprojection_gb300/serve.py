@@ -115,7 +115,7 @@ class ServingReport:
                 "wall_s": self.wall_s, "pixel_pulses": work,
                 "gpix_pulse_per_s": work / self.wall_s / 1e9 if self.wall_s > 0 else None,
                 "waves": self.waves, "gpu_launches": self.gpu_launches,
-                "peak_resident_gb": self.peak_bytes / GB}
+                "peak_resident_gb": self.peak_bytes / GB if self.peak_bytes else None}
 
 
 class ServingEngine:
@@ -455,6 +455,163 @@ class NativeQueue:
             rc = int(self.lib.sarbp_queue_destroy(self._q))
             self._q = C.c_void_p()
             self._keep.clear()
+            _lib.check(rc)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def _host_grid(a, np_dtype):
+    """(owner, pointer) of a host DEM-grid array as column-major ``np_dtype``
+    data: the array itself when it already is (a NumPy F-order array or a
+    CPU tensor whose transpose is contiguous, pinned memory kept), else a
+    column-major copy."""
+    if isinstance(a, torch.Tensor):
+        tdt = getattr(torch, np.dtype(np_dtype).name)
+        if a.device.type == "cpu" and a.dtype == tdt and (a.dim() != 2 or a.t().is_contiguous()):
+            return a, a.data_ptr()
+        a = a.detach().cpu().numpy()
+    arr = np.asarray(a)
+    if not (arr.dtype == np_dtype and (arr.ndim != 2 or arr.flags.f_contiguous)):
+        arr = np.asfortranarray(arr.astype(np_dtype))
+    return arr, arr.ctypes.data
+
+
+def _host_vector(w, naz: int):
+    """(owner, pointer) of a trajectory component as ``naz`` contiguous float64
+    (the reference reads pulses 0 < a < Naz-1 only: a shorter trajectory of
+    Naz-1 points is padded with its last point)."""
+    if isinstance(w, torch.Tensor) and w.device.type == "cpu" and w.dtype == torch.float64 \
+            and w.is_contiguous() and w.numel() >= naz:
+        return w, w.data_ptr()
+    v = np.ascontiguousarray(np.asarray(w, dtype=np.float64).reshape(-1))
+    if v.size < naz:
+        v = np.concatenate([v, np.full(naz - v.size, v[-1] if v.size else 0.0)])
+    return v, v.ctypes.data
+
+
+def host_scene(args: tuple) -> tuple:
+    """The 13 focusing arguments as a host sarbp_scene (pointers into the
+    caller's arrays where their layout allows, else into column-major
+    copies); returns (scene struct, owners to keep alive)."""
+    (xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, raw, near, dra, lam, sint) = args
+    if len(tuple(raw.shape)) != 2 or len(tuple(xxg1.shape)) != 2:
+        raise ValueError("Raw_Data and xxg1 must be 2D arrays")
+    dim0, dim1 = (int(v) for v in xxg1.shape)
+    nra, naz = (int(v) for v in raw.shape)
+    keep = []
+    ptr = {}
+    for name, a, dt in (("dem_x", xxg1, np.float64), ("dem_y", yyg1, np.float64),
+                        ("dem_z", zzg1, np.float64), ("mask", mask, np.uint8),
+                        ("index", index, np.int32), ("sint", sint, np.int32)):
+        if int(np.prod(tuple(a.shape))) != dim0 * dim1:
+            raise ValueError(f"{name} does not match the DEM grid")
+        o, p = _host_grid(a, dt)
+        keep.append(o)
+        ptr[name] = p
+    for name, w in (("traj_x", wgsx), ("traj_y", wgsy), ("traj_z", wgsz)):
+        if int(np.prod(tuple(w.shape))) < naz - 1:
+            raise ValueError(f"{name} has fewer than Naz-1 points")
+        o, p = _host_vector(w, naz)
+        keep.append(o)
+        ptr[name] = p
+    o, p = _host_grid(raw, np.complex64)                  # (nra, naz) column-major rows
+    keep.append(o)
+    sc = _lib.Scene(dim0=dim0, dim1=dim1, nra=nra, naz=naz, raw_pitch=nra,
+                    near_range=float(near), delta_range=float(dra), lambda_=float(lam),
+                    raw=p, **ptr)
+    return sc, keep
+
+
+class NativeServingEngine:
+    """Continuous batching with the whole request path in the C queue's worker
+    thread (sarbp_queue_submit_host): jobs are submitted from host memory at
+    their arrival times; admission by slot and reserved device memory, the
+    small uploads, chunk tables, reachable-bin bound, raw upload, waves and
+    the image read-back all run natively.  The Python loop only submits and
+    drains completions (sarbp_queue_completed), whose times come from the
+    worker (the monotonic clock).  Images are bit-identical to the
+    single-scene staged kernel's."""
+
+    def __init__(self, device=None, budget_bytes: int = 150 * GB, max_slots: int = 32,
+                 wave_items: int = 0, tuning=None):
+        self.device = torch.device(device or "cuda")
+        self.lib = _lib.load()
+        self.tuning = staged_tuning() if tuning is None else resolve_tuning(tuning)
+        self.budget = int(budget_bytes)
+        self._q = C.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.sarbp_queue_create(C.byref(self._q), C.byref(self.tuning),
+                                                   int(max_slots), int(wave_items)))
+            try:
+                _lib.check(self.lib.sarbp_queue_reserve(self._q, self.budget))
+            except Exception:
+                self.lib.sarbp_queue_destroy(self._q)
+                raise
+
+    def job_bytes(self, args) -> int:
+        sc, _ = host_scene(args)
+        return _lib.check(int(self.lib.sarbp_queue_job_bytes(self._q, C.byref(sc))))
+
+    def run(self, jobs: list, idle_sleep: float = 5e-5, timeout_s: float = 600.0):
+        """Submit every job at its arrival time (seconds after the start),
+        wait for all; returns a ServingReport (``waves``/``gpu_launches``
+        are not counted by the native worker: None)."""
+        prepared = []
+        for j in sorted(jobs, key=lambda j: j.arrival):     # outside the timed loop
+            sc, keep = host_scene(j.args)
+            out = torch.empty((sc.dim0 * sc.dim1, 2), dtype=torch.float64, pin_memory=True)
+            if not j.nominal:
+                j.nominal = _nominal(j.args)
+            prepared.append((j, sc, keep, out))
+        byid = {}
+        ids = (C.c_int64 * 256)()
+        times = (C.c_double * 256)()
+        stat = (C.c_int32 * 256)()
+        gc_was_enabled = gc.isenabled()
+        gc.disable()
+        try:
+            t0 = time.monotonic()
+            nxt, done = 0, 0
+            while done < len(prepared):
+                now = time.monotonic() - t0
+                if now > timeout_s:
+                    raise TimeoutError(f"serving run exceeded {timeout_s} s")
+                while nxt < len(prepared) and prepared[nxt][0].arrival <= now:
+                    j, sc, keep, out = prepared[nxt]
+                    jid = _lib.check(int(self.lib.sarbp_queue_submit_host(
+                        self._q, C.byref(sc), out.data_ptr())))
+                    j.admitted = now
+                    byid[jid] = prepared[nxt]
+                    nxt += 1
+                n = _lib.check(int(self.lib.sarbp_queue_completed(self._q, ids, times, stat,
+                                                                  256)))
+                for k in range(n):
+                    j, sc, keep, out = byid.pop(ids[k])
+                    _lib.check(int(stat[k]))
+                    j.finished = times[k] - t0
+                    flat = out.numpy().view(np.complex128).reshape(-1)
+                    j.image = np.reshape(flat, (sc.dim0, sc.dim1), order="F")
+                done += n
+                if n == 0 and idle_sleep:
+                    wait = idle_sleep
+                    if nxt < len(prepared):
+                        wait = min(wait, max(0.0, prepared[nxt][0].arrival - now))
+                    time.sleep(wait)
+            wall = time.monotonic() - t0
+        finally:
+            if gc_was_enabled:
+                gc.enable()
+        return ServingReport(jobs=jobs, wall_s=wall, waves=None, gpu_launches=None,
+                             peak_bytes=0)
+
+    def close(self) -> None:
+        if self._q:
+            rc = int(self.lib.sarbp_queue_destroy(self._q))
+            self._q = C.c_void_p()
             _lib.check(rc)
 
     def __enter__(self):

@@ -173,3 +173,9 @@ def test_new_entry_points_reject_bad_arguments_without_a_gpu():
     assert "staged = 1" in _lib.last_error()
     assert lib.sarbp_queue_submit(None, C.byref(s), out) == _lib.SARBP_EINVAL
     assert lib.sarbp_queue_destroy(None) == _lib.SARBP_OK
+    # host-memory jobs: NULL queue / output, nothing to reserve
+    assert lib.sarbp_queue_reserve(None, 1 << 20) == _lib.SARBP_EINVAL
+    assert lib.sarbp_queue_job_bytes(None, C.byref(s)) == _lib.SARBP_EINVAL
+    assert lib.sarbp_queue_submit_host(None, C.byref(s), out) == _lib.SARBP_EINVAL
+    ids = (C.c_int64 * 4)()
+    assert lib.sarbp_queue_completed(None, ids, None, None, 4) == _lib.SARBP_EINVAL

@@ -71,3 +71,48 @@ def test_budget_limits_residency(jobs):
 def test_fp64_sequential_comparator(jobs):
     r = serve.run_fp64_sequential(jobs[:3])
     assert r["p99_ms"] >= r["p50_ms"] > 0 and r["pixel_pulses"] > 0
+
+
+def _pinned(args):
+    """The same job with page-locked inputs (torch pin_memory), the layout
+    the native queue reads by SM loads."""
+    out = list(args)
+    for i in (0, 1, 2, 3, 4, 8, 12):
+        a = np.asarray(args[i])
+        out[i] = torch.from_numpy(np.ascontiguousarray(a.T)).pin_memory().t()
+    for i in (5, 6, 7):
+        out[i] = torch.from_numpy(np.ascontiguousarray(args[i])).pin_memory()
+    return tuple(out)
+
+
+@pytest.mark.parametrize("memory", ["pageable", "pinned"])
+def test_native_engine_each_job_same_alone_and_in_the_mix(jobs, memory):
+    """The whole request path in the C queue's worker (host inputs in, host
+    image out): every job's image equals its single-scene image bit for bit."""
+    tuning = batch.staged_tuning()
+    mine = [serve.Job(job_id=j.job_id, arrival=j.arrival,
+                      args=_pinned(j.args) if memory == "pinned" else j.args) for j in jobs]
+    with serve.NativeServingEngine(budget_bytes=8 * serve.GB, max_slots=8, wave_items=96,
+                                   tuning=tuning) as eng:
+        rep = eng.run(mine)
+    s = rep.summary()
+    assert s["completed"] == len(jobs) and s["p99_ms"] >= s["p50_ms"] > 0
+    for j, ref in zip(mine, jobs):
+        assert j.image is not None and j.image.shape == ref.shape
+        assert np.array_equal(_bits(j.image), _bits(_alone(ref, tuning))), f"job {j.job_id}"
+
+
+def test_native_engine_reserved_memory_limits_residency(jobs):
+    """A reserve that holds one job at a time still completes every job; a
+    job larger than the whole reserve is refused at submission."""
+    small = [serve.Job(job_id=j.job_id, arrival=0.0, args=j.args) for j in jobs[:4]]
+    probe = serve.NativeServingEngine(budget_bytes=1 << 30, max_slots=4)
+    need = max(probe.job_bytes(j.args) for j in small)
+    probe.close()
+    with serve.NativeServingEngine(budget_bytes=need, max_slots=4, wave_items=64) as eng:
+        rep = eng.run(small)
+        assert rep.summary()["completed"] == len(small)
+    with serve.NativeServingEngine(budget_bytes=need // 4, max_slots=4) as eng:
+        with pytest.raises(Exception) as e:
+            eng.run(small[:1], timeout_s=30)
+        assert "reserved" in str(e.value)
