@@ -401,6 +401,26 @@ def run_serving(args, dev):
     eng = serve.ServingEngine(device=dev, budget_bytes=150 * serve.GB, max_slots=32)
     py_sat = eng.run(make(np.zeros(args.serve_jobs))).summary()
     del eng
+    # the link the saturated run is bound by: SM-load copies from pinned memory
+    import ctypes as C
+
+    from sar_backprojection_gb300 import _lib
+    lib = _lib.load()
+    src = torch.empty(1 << 30, dtype=torch.uint8, pin_memory=True)
+    dst = torch.empty(1 << 30, dtype=torch.uint8, device=dev)
+    sp = torch.cuda.current_stream(dev).cuda_stream
+    for _ in range(2):
+        _lib.check(lib.sarbp_copy_to_device_sm(dst.data_ptr(), src.data_ptr(), src.numel(), sp))
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(5):
+        _lib.check(lib.sarbp_copy_to_device_sm(dst.data_ptr(), src.data_ptr(), src.numel(), sp))
+    b.record()
+    torch.cuda.synchronize(dev)
+    link = 5 * src.numel() / (a.elapsed_time(b) * 1e-3) / 1e9
+    del src, dst
+    sat["link_gb_per_s"] = link
+    sat["link_frac"] = sat["h2d_gb_per_s"] / link if sat.get("h2d_gb_per_s") else None
     f64 = serve.run_fp64_sequential(make(serve.poisson_arrivals(args.serve_jobs, 0.5 * cap,
                                                                 seed=7)), device=dev)
     f64["jobs"] = args.serve_jobs
@@ -412,6 +432,138 @@ def run_serving(args, dev):
             "what": "latency = arrival to image in host memory (completion time taken by the "
                     "queue's worker); inputs in pinned host memory, uploaded per job by SM "
                     "loads (small inputs, then the reachable range bins)"}
+
+
+def _scratch_dir(need_bytes: int):
+    """A directory on a file system with ``need_bytes`` free (plus 8 GB), or None."""
+    import shutil
+    cands = [os.environ.get("TMPDIR"), "/tmp", "/dev/shm", str(ROOT)]
+    for c in cands:
+        if not c or not os.path.isdir(c):
+            continue
+        try:
+            if shutil.disk_usage(c).free >= need_bytes + (8 << 30):
+                return tempfile.mkdtemp(prefix="sarbp_large_", dir=c)
+        except OSError:
+            continue
+    return None
+
+
+def _bits(a) -> np.ndarray:
+    """The bytes of an array (any layout) as uint64 words, column-major."""
+    return np.asfortranarray(np.asarray(a)).reshape(-1, order="F").view(np.uint64)
+
+
+def _host_available_bytes() -> int:
+    try:
+        return os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
+    except (ValueError, OSError):
+        return 0
+
+
+def run_large_scene(args, dev, tuning):
+    """The large-scene driver at the reference's size (DEM 4000 x 32000,
+    RawData 4762 x 403484 = 15.4 GB; main_gpu.py:321-324): seeded synthetic
+    .dat files written to local disk, then focused file to memory-mapped
+    output (timed, wall clock), then again with an interruption and resume
+    and the diagnostic outputs, checked against the first run bit for bit
+    and against the oracle on a seeded pixel sample."""
+    import shutil
+
+    import torch
+
+    from oracle import oracle
+    from sar_backprojection_gb300 import datfiles, quality, synth
+    from sar_backprojection_gb300.large_scene import Cursor, LargeSceneFocuser
+
+    spec = synth.large_spec()
+    dim_rg, dim_az, nra, naz = spec.dim1, spec.dim0, spec.nra, spec.naz
+    npix = dim_rg * dim_az
+    need = nra * naz * 8 + npix * (29 + 16 + 16 + 12)
+    if _host_available_bytes() < (48 << 30):
+        return {"skipped": "less than 48 GB of free host memory"}
+    d = _scratch_dir(need)
+    if d is None:
+        return {"skipped": f"no file system with {need / 1e9:.0f} GB free"}
+    res = {"workload": f"DEM {dim_rg} x {dim_az} (azimuth along the second axis), "
+                       f"RawData {nra} x {naz} ({nra * naz * 8 / 1e9:.1f} GB complex64), "
+                       "Sint 1200..1800, 80% mask, 2000 point targets + clutter",
+           "dir_fs": d}
+    try:
+        t0 = time.perf_counter()
+        g = synth.generate(spec, raw_device=str(dev))
+        work = synth.nominal_pixel_pulses(g)
+        sc = synth.azimuth_columns(g)
+        del g
+        datfiles.save_scene(d, sc)
+        del sc
+        torch.cuda.synchronize(dev)
+        torch.cuda.empty_cache()
+        res["generate_and_write_s"] = time.perf_counter() - t0
+        out1 = Path(d) / "slc_a.dat"
+        lf = LargeSceneFocuser(out1, batch_cols=2000, tuning=tuning, device=dev)
+        t0 = time.perf_counter()
+        img1 = lf.focus_files(d, dim_rg, dim_az, nra, naz)
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - t0
+        torch.cuda.empty_cache()
+        res.update({"nominal_pixel_pulses": int(work), "wall_s": wall,
+                    "host_phases_s": dict(lf.timing),
+                    "value": work / wall / 1e9, "unit": UNIT, "launches": lf.launches,
+                    "batches": (dim_az + 1999) // 2000, "batch_cols": 2000,
+                    "tuning": tuning.as_dict(),
+                    "what": "focus_files: memory-mapped .dat inputs (page cache warm: written "
+                            "just before), raw data streamed to HBM through pinned buffers, "
+                            "one launch per 2000-column batch, image written to a "
+                            "memory-mapped complex128 file, cursor saved per batch"})
+        # interrupted after 5 batches, resumed, with the diagnostic outputs
+        out2 = Path(d) / "slc_b.dat"
+        lf2 = LargeSceneFocuser(out2, batch_cols=2000, tuning=tuning, device=dev,
+                                diagnostics=True)
+        lf2.focus_files(d, dim_rg, dim_az, nra, naz, max_batches=5)
+        stopped_at = Cursor.load(str(out2) + ".cursor").next_batch
+        lf3 = LargeSceneFocuser(out2, batch_cols=2000, tuning=tuning, device=dev,
+                                diagnostics=True)
+        t0 = time.perf_counter()
+        img2 = lf3.focus_files(d, dim_rg, dim_az, nra, naz)
+        torch.cuda.synchronize(dev)
+        res["resume"] = {"stopped_after_batches": stopped_at,
+                         "resumed_wall_s": time.perf_counter() - t0,
+                         "equals_uninterrupted_run": bool(all(
+                             np.array_equal(_bits(img1[:, c:c + 2000]), _bits(img2[:, c:c + 2000]))
+                             for c in range(0, dim_az, 2000)))}
+        torch.cuda.empty_cache()
+        # the oracle on a seeded pixel sample of the files
+        names = datfiles.scene_filenames(dim_rg, dim_az, nra, naz)
+        mm = {k: np.memmap(Path(d) / names[k], dtype=dt, mode="r", shape=(dim_rg, dim_az),
+                           order="F")
+              for k, dt in (("xxg1", np.float64), ("yyg1", np.float64), ("zzg1", np.float64),
+                            ("Mask", np.uint8), ("Index", np.int32), ("Sint", np.int32))}
+        traj = [datfiles.read_dat(Path(d) / names[k], np.float64) for k in ("wgsx", "wgsy", "wgsz")]
+        raw = datfiles.open_raw_memmap(Path(d) / names["RawData"], nra, naz)
+        rng = np.random.default_rng(2024)
+        pix = np.sort(rng.choice(npix, 4000, replace=False))
+        t0 = time.perf_counter()
+        ov, onv, ocs = oracle.focus(mm["xxg1"], mm["yyg1"], mm["zzg1"], mm["Mask"], mm["Index"],
+                                    *traj, raw, spec.near_range, spec.delta_range,
+                                    spec.wavelength, mm["Sint"], pixels=pix,
+                                    nthreads=len(os.sched_getaffinity(0)))
+        i0, i1 = pix % dim_rg, pix // dim_rg
+        gv = np.asarray(img2)[i0, i1]
+        q = quality.compare(gv, ov)
+        res["oracle_sample"] = {
+            "pixels": int(pix.size), "seconds": time.perf_counter() - t0,
+            "counts_bit_exact": bool(np.array_equal(np.asarray(lf3.nvalid)[i0, i1], onv)),
+            "checksums_bit_exact": bool(np.array_equal(np.asarray(lf3.checksum)[i0, i1], ocs)),
+            "coherence": q["coherence"], "rms_phase_mrad": q["rms_phase_mrad"],
+            "rel_l2": q["rel_l2"]}
+        del img1, img2, mm, raw
+    except Exception as e:         # reported, never fatal to the bench line
+        res["error"] = f"{type(e).__name__}: {e}"
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+        torch.cuda.empty_cache()
+    return res
 
 
 TUNING_FIELDS = ("chunk", "tile0", "tile1", "staged", "window", "stage")
@@ -540,6 +692,20 @@ def run_ours(args, dist: Dist):
     ms_per_step = elapsed_ms / args.steps
     value = dist.world * work / (ms_per_step * 1e-3) / 1e9
     gpu_launches = 2 * args.steps
+
+    # the same scene through the persistent batch kernel (one graph replay per
+    # step: chunk tables + the persistent launch over the scene's tile queue)
+    from sar_backprojection_gb300 import batch as _batch
+    bsingle = _batch.BatchFocuser([ds], tuning, graph=True)
+    for _ in range(3):
+        bsingle.run()
+    b_ms = _batch.time_steps(bsingle.run, max(5, args.steps // 4), dev)
+    b_same = bool(torch.equal(bsingle.slots[0].out, out))
+    batched_kernel = {"value": work / (b_ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": b_ms,
+                      "image_equals_single_scene_kernel": b_same,
+                      "what": "the full scene as a one-scene batch: persistent grid over its "
+                              "(scene, tile) queue, chunk tables and launch in one CUDA graph"}
+    del bsingle
 
     # the plain FP64 kernel on the same scene (comparator), and quality
     mixed_img = out.clone()
@@ -735,6 +901,9 @@ def run_ours(args, dist: Dist):
             "fp64": ({"value": dist.world * work / (fp64_ms * 1e-3) / 1e9, "unit": UNIT,
                       "ms_per_step": fp64_ms, "steps": args.fp64_steps} if fp64_ms else None),
             "speedup_mixed_vs_fp64": fp64_ms / ms_per_step if fp64_ms else None,
+            "batched_kernel": batched_kernel,
+            "speedup_batched_vs_fp64": (fp64_ms / batched_kernel["ms_per_step"]
+                                        if fp64_ms else None),
             "quality": ({"vs": "FP64 kernel (bit-exact bins with the oracle)",
                          "coherence": q["coherence"], "rms_phase_mrad": q["rms_phase_mrad"],
                          "rel_l2": q["rel_l2"], "bins_bit_exact": bins_exact,

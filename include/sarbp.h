@@ -390,6 +390,13 @@ SARBP_API int64_t sarbp_queue_submit_host(sarbp_queue *queue, const sarbp_scene 
                                           double *host_out);
 SARBP_API int64_t sarbp_queue_completed(sarbp_queue *queue, int64_t *ids, double *done_s,
                                         int32_t *status, int64_t max);
+/*
+ * Totals since the queue was created, into stats[0..4]: jobs completed,
+ * waves launched, kernel launches (waves, and for host jobs their copies,
+ * chunk tables, bound and batch-slot kernels), bytes copied host -> device
+ * and device -> host for host jobs.  No reference counterpart.
+ */
+SARBP_API int sarbp_queue_stats(sarbp_queue *queue, int64_t *stats);
 
 /*
  * 8-bit amplitude preview of a focused image: out[i] = clip(|image[i]| *

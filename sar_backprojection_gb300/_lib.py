@@ -86,6 +86,7 @@ SIGNATURES = {
     "sarbp_queue_reserve": (C.c_int, [_P, C.c_size_t]),
     "sarbp_queue_job_bytes": (C.c_int64, [_P, C.POINTER(Scene)]),
     "sarbp_queue_submit_host": (C.c_int64, [_P, C.POINTER(Scene), _P]),
+    "sarbp_queue_stats": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "sarbp_queue_completed": (C.c_int64, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_double),
                                           C.POINTER(C.c_int32), C.c_int64]),
     "sarbp_tile_queue_keys": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, C.c_size_t,

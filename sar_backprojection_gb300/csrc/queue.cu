@@ -187,6 +187,9 @@ struct Queue {
     std::unordered_map<int64_t, std::unique_ptr<QJob>> jobs;
     std::vector<int> free_slots;
     std::deque<Wave> waves;
+    // totals since creation: completed jobs, waves, kernel launches, bytes
+    // copied host -> device and device -> host
+    int64_t stat_jobs = 0, stat_waves = 0, stat_launches = 0, stat_h2d = 0, stat_d2h = 0;
     unsigned *wave_error = nullptr;   // mapped pinned: batch status per turn
     unsigned *wave_error_dev = nullptr;
     int64_t next_id = 0;
@@ -287,6 +290,11 @@ int Queue::admit_host(QJob &j)
     }
     rc = raw_bin_range_async(D, T, j.ws, j.ws_bytes, bounds + 2 * j.slot, setup);
     if (rc) return rc;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        stat_launches += 9 + 1 + 3 + 2;   // copies, chunk table, bound, batch slot x2
+        stat_h2d += 33 * npix + 24 * naz;
+    }
     rc = queue_cuda(cudaEventCreateWithFlags(&j.ev, cudaEventDisableTiming), "queue: job event");
     if (rc) return rc;
     rc = queue_cuda(cudaEventRecord(j.ev, setup), "queue: set-up record");
@@ -317,9 +325,13 @@ bool Queue::advance_host()
         int rc = queue_cuda(q, "queue: job step");
         if (!rc && j.stage == kSetup) {
             const int32_t lo = bounds[2 * j.slot], hi = bounds[2 * j.slot + 1];
-            if (hi >= lo)
+            if (hi >= lo) {
                 rc = h2d_rows(const_cast<float2 *>(j.P.raw), j.P.pitch, j.H.raw, j.H.pitch, lo,
                               (int64_t)hi - lo + 1, j.H.naz, copy);
+                std::lock_guard<std::mutex> lk(mu);
+                stat_launches += 1;
+                stat_h2d += 8 * ((int64_t)hi - lo + 1) * j.H.naz;
+            }
             if (!rc) rc = queue_cuda(cudaEventRecord(j.ev, copy), "queue: upload record");
             if (!rc) {
                 j.stage = kUpload;
@@ -359,6 +371,7 @@ void Queue::finish(QJob &j)
     j.slot = -1;
     j.done = true;
     j.done_s = steady_seconds();
+    stat_jobs += 1;
     // ids already reported through poll/wait are dropped from the front
     while (completions.size() > 4096 && !jobs.count(completions.front())) completions.pop_front();
     completions.push_back(j.id);
@@ -412,6 +425,8 @@ int Queue::launch_wave(bool *launched)
     if (rc) return rc;
     waves.push_back(std::move(w));
     *launched = true;
+    stat_waves += 1;
+    stat_launches += 2;   // persistent batch kernel, status word
     return SARBP_OK;
 }
 
@@ -445,6 +460,8 @@ int Queue::retire_waves(bool *retired)
                     }
                     // the image goes back to the caller's host buffer
                     int rc2 = d2h_bytes(j.host_out, j.out, 16 * j.P.npix, readback);
+                    stat_launches += 1;
+                    stat_d2h += 16 * j.P.npix;
                     if (!rc2) rc2 = queue_cuda(cudaEventRecord(j.ev, readback),
                                                "queue: read-back record");
                     if (rc2) {
@@ -713,6 +730,22 @@ SARBP_API int64_t sarbp_queue_submit_host(sarbp_queue *queue, const sarbp_scene 
     }
     q.cv.notify_one();
     return id;
+}
+
+SARBP_API int sarbp_queue_stats(sarbp_queue *queue, int64_t *stats)
+{
+    if (!queue || !stats) {
+        set_error("sarbp_queue_stats: queue or stats is NULL");
+        return SARBP_EINVAL;
+    }
+    Queue &q = queue->q;
+    std::lock_guard<std::mutex> lk(q.mu);
+    stats[0] = q.stat_jobs;
+    stats[1] = q.stat_waves;
+    stats[2] = q.stat_launches;
+    stats[3] = q.stat_h2d;
+    stats[4] = q.stat_d2h;
+    return SARBP_OK;
 }
 
 SARBP_API int64_t sarbp_queue_completed(sarbp_queue *queue, int64_t *ids, double *done_s,

@@ -104,6 +104,8 @@ class ServingReport:
     gpu_launches: int
     peak_bytes: int
     latencies_ms: list = field(default_factory=list)
+    h2d_bytes: int | None = None          # native engine: bytes uploaded / read back
+    d2h_bytes: int | None = None
 
     def summary(self) -> dict:
         lat = np.array([j.latency for j in self.jobs if j.latency is not None]) * 1e3
@@ -115,7 +117,11 @@ class ServingReport:
                 "wall_s": self.wall_s, "pixel_pulses": work,
                 "gpix_pulse_per_s": work / self.wall_s / 1e9 if self.wall_s > 0 else None,
                 "waves": self.waves, "gpu_launches": self.gpu_launches,
-                "peak_resident_gb": self.peak_bytes / GB if self.peak_bytes else None}
+                "peak_resident_gb": self.peak_bytes / GB if self.peak_bytes else None,
+                "h2d_gb": self.h2d_bytes / 1e9 if self.h2d_bytes is not None else None,
+                "d2h_gb": self.d2h_bytes / 1e9 if self.d2h_bytes is not None else None,
+                "h2d_gb_per_s": (self.h2d_bytes / 1e9 / self.wall_s
+                                 if self.h2d_bytes is not None and self.wall_s > 0 else None)}
 
 
 class ServingEngine:
@@ -568,6 +574,7 @@ class NativeServingEngine:
                 j.nominal = _nominal(j.args)
             prepared.append((j, sc, keep, out))
         byid = {}
+        before = self.stats()
         ids = (C.c_int64 * 256)()
         times = (C.c_double * 256)()
         stat = (C.c_int32 * 256)()
@@ -605,8 +612,18 @@ class NativeServingEngine:
         finally:
             if gc_was_enabled:
                 gc.enable()
-        return ServingReport(jobs=jobs, wall_s=wall, waves=None, gpu_launches=None,
-                             peak_bytes=0)
+        after = self.stats()
+        rep = ServingReport(jobs=jobs, wall_s=wall, waves=after["waves"] - before["waves"],
+                            gpu_launches=after["launches"] - before["launches"], peak_bytes=0)
+        rep.h2d_bytes = after["h2d_bytes"] - before["h2d_bytes"]
+        rep.d2h_bytes = after["d2h_bytes"] - before["d2h_bytes"]
+        return rep
+
+    def stats(self) -> dict:
+        """The queue's totals (sarbp_queue_stats)."""
+        v = (C.c_int64 * 5)()
+        _lib.check(self.lib.sarbp_queue_stats(self._q, v))
+        return dict(zip(("jobs", "waves", "launches", "h2d_bytes", "d2h_bytes"), list(v)))
 
     def close(self) -> None:
         if self._q:
