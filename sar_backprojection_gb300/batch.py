@@ -31,6 +31,27 @@ STAGED_TILINGS = ((16, 16, 208, 64), (16, 16, 208, 128), (16, 16, 160, 128), (16
                   (16, 8, 128, 128), (32, 8, 128, 64))
 
 
+ORDERS = ("cost", "bucket", "natural")
+
+
+def item_order(cost: torch.Tensor, how: str = "cost", buckets: int = 8) -> torch.Tensor:
+    """Processing order of the (scene, tile) items listed scene by scene in
+    natural tile order: "cost" by decreasing estimated cost (the longest
+    items start first, so no wave ends half empty); "bucket" by decreasing
+    cost class (``buckets`` classes of equal width up to the largest cost),
+    natural order within a class, so neighbouring tiles, whose raw windows
+    overlap, still run close together in time and share L2; "natural" as
+    listed."""
+    n = cost.numel()
+    if how == "natural" or n == 0:
+        return torch.arange(n, device=cost.device)
+    if how == "cost":
+        return torch.argsort(cost, descending=True, stable=True)
+    top = max(int(cost.max().item()), 1)
+    cls = torch.clamp(cost * buckets // (top + 1), max=buckets - 1)
+    return torch.argsort(-cls, stable=True)
+
+
 def staged_tuning(tile0: int = 16, tile1: int = 16, window: int = 208, chunk: int = 64,
                   stage: int = 32) -> _lib.Tuning:
     return resolve_tuning({"chunk": chunk, "tile0": tile0, "tile1": tile1, "staged": 1,
@@ -62,7 +83,7 @@ class BatchFocuser:
     """
 
     def __init__(self, scenes: list[DeviceScene], tuning=None, diagnostics: bool = False,
-                 graph: bool = True):
+                 graph: bool = True, order: str = "cost"):
         if not scenes:
             raise ValueError("BatchFocuser needs at least one scene")
         self.lib = _lib.load()
@@ -73,6 +94,9 @@ class BatchFocuser:
         # the batch has its own (scene, tile) queue: no per-scene tile queue
         self.tuning.staged = 1
         self.diagnostics = diagnostics
+        if order not in ORDERS:
+            raise ValueError(f"order must be one of {ORDERS}")
+        self.order = order
         self.counters = (torch.zeros(_lib.NUM_COUNTERS, dtype=torch.int64, device=self.device)
                          if diagnostics else None)
         tb = C.byref(self.tuning)
@@ -134,7 +158,7 @@ class BatchFocuser:
             slot_ids.append(torch.full((sl.ntiles,), i, dtype=torch.int32, device=self.device))
             tile_ids.append(torch.arange(sl.ntiles, dtype=torch.int32, device=self.device))
         cost = torch.cat(costs)
-        order = torch.argsort(cost, descending=True, stable=True)
+        order = item_order(cost, self.order)
         items = torch.stack([torch.cat(slot_ids)[order], torch.cat(tile_ids)[order]], dim=1)
         self.items = items.to(torch.int32).cpu().contiguous()
         self.total_cost = int(cost.sum().item())

@@ -229,6 +229,7 @@ struct BatchScene {
     TileOutputs outputs;
     int64_t ntile0, ntiles;
 };
+static_assert(sizeof(BatchScene) % 16 == 0, "scene records copy as 16-byte words");
 
 // Focus one pixel tile; false if a bounded wait gave up (the CTA must stop).
 // Every thread of the CTA calls it with the same tile.
@@ -827,6 +828,9 @@ focus_batch_staged_kernel(const BatchScene *__restrict__ scenes, const int2 *__r
 {
     extern __shared__ unsigned char smem_dyn[];
     __shared__ StagedShared sh;
+    // the current item's scene record (parameters, tables, outputs): read
+    // from shared memory by the tile code instead of from global memory
+    __shared__ __align__(16) unsigned char srec[sizeof(BatchScene)];
     StagedCta cta = staged_cta_init<Cfg>(smem_dyn, sh);
     TileStats st{0, 0, 0};
     for (int round = 0;; ++round) {
@@ -835,9 +839,18 @@ focus_batch_staged_kernel(const BatchScene *__restrict__ scenes, const int2 *__r
         const long long item = sh.item[round & 1];
         if (item >= n_items) break;
         const int2 w = items[item];
-        const BatchScene &B = scenes[w.x];
+        const BatchScene &G = scenes[w.x];
+        {
+            // every thread is past the previous tile (the barrier above)
+            const uint4 *src = reinterpret_cast<const uint4 *>(&G);
+            uint4 *dst = reinterpret_cast<uint4 *>(srec);
+            for (int k = threadIdx.x; k < (int)(sizeof(BatchScene) / 16); k += blockDim.x)
+                dst[k] = src[k];
+        }
+        __syncthreads();
+        const BatchScene &B = *reinterpret_cast<const BatchScene *>(srec);
         const int64_t tile = w.y;
-        const bool ok = staged_tile<Cfg, kChecksum>(cta, B.P, &B.map, B.tables,
+        const bool ok = staged_tile<Cfg, kChecksum>(cta, B.P, &G.map, B.tables,
                                                     tile % B.ntile0, tile / B.ntile0,
                                                     B.outputs, st);
         if (!ok) {

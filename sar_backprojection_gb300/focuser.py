@@ -152,6 +152,13 @@ def FocalizzatoreBpPx(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
 
 
 STREAM_BLOCKS = 8      # pulse blocks of a streamed drop-in upload
+# how the streamed drop-in copies the reachable raw bins from page-locked
+# host memory: "sm" (SM loads on a high-priority stream, whose CTAs take SMs
+# as focusing CTAs finish) or "copy" (copy engine).  Measured over 450 calls
+# each on the full workload: SM loads 3.99 ms mean, 4.01 ms median, 4.19 ms
+# worst; the copy engine 3.91 ms mean, 3.35 ms median but 24 ms at the 99th
+# percentile and 75 ms worst (its host-to-device stalls)
+STREAM_UPLOAD = "sm"
 IMAGE_POOL = 4         # host images the drop-in call keeps for reuse
 
 
@@ -205,6 +212,7 @@ class _DropIn:
         import threading
         self.lock = threading.Lock()
         self.copy = torch.cuda.Stream(dev)
+        self.copy_sm = torch.cuda.Stream(dev, priority=torch.cuda.Stream.priority_range()[1])
         self.side = torch.cuda.Stream(dev)
         self.raw: dict[tuple, torch.Tensor] = {}
         self.out: dict[int, torch.Tensor] = {}
@@ -283,7 +291,9 @@ def _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache: _DropIn):
     marks += [naz - naz // (2 * blocks), naz]
     ends = np.searchsorted(keys, np.asarray(marks, dtype=np.int64), side="right")
     ends[-1] = nt
-    copy = res_cache.copy
+    sm = STREAM_UPLOAD == "sm" and scene.host_rows.is_pinned()
+    copy = res_cache.copy_sm if sm else res_cache.copy
+    upload = lib.sarbp_upload_raw_bins_sm if sm else lib.sarbp_upload_raw_bins
     copy.wait_stream(compute)               # raw buffer and tables allocated on compute
     # segments alternate between two compute streams so that one segment's
     # last CTAs overlap the next segment's first
@@ -297,7 +307,7 @@ def _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache: _DropIn):
     for k in range(len(marks)):
         a1 = marks[k]
         if hi >= lo and a1 > a0:
-            _lib.check(lib.sarbp_upload_raw_bins(
+            _lib.check(upload(
                 scene.raw.data_ptr() + a0 * row, scene.pitch,
                 scene.host_rows.data_ptr() + a0 * scene.nra * 8, scene.nra, lo, hi - lo + 1,
                 a1 - a0, copy.cuda_stream))

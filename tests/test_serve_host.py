@@ -54,3 +54,15 @@ def test_summary_percentiles():
     s = rep.summary()
     assert s["p50_ms"] == pytest.approx(50.5) and s["p99_ms"] == pytest.approx(99.01)
     assert s["pixel_pulses"] == 10000 and s["peak_resident_gb"] == 1.0
+
+
+def test_batch_item_orders():
+    """Work-queue orders of the batch kernel: decreasing cost, decreasing cost
+    class with the natural tile order inside a class, natural."""
+    import torch
+    from sar_backprojection_gb300.batch import item_order
+    c = torch.tensor([5, 1, 9, 9, 2, 8, 0])
+    assert item_order(c, "cost").tolist() == [2, 3, 5, 0, 4, 1, 6]
+    assert item_order(c, "bucket", buckets=4).tolist() == [2, 3, 5, 0, 1, 4, 6]
+    assert item_order(c, "natural").tolist() == list(range(7))
+    assert item_order(torch.tensor([], dtype=torch.int64), "bucket").numel() == 0
