@@ -69,7 +69,14 @@ struct StagedCfg {
     static constexpr size_t raw_bytes = (size_t)STAGE * W * sizeof(float2);
     static constexpr size_t tab_bytes = (size_t)STAGE * sizeof(float4);
     static constexpr size_t buf_bytes = raw_bytes + tab_bytes;
-    static constexpr size_t smem_bytes = NBUF * buf_bytes + 128;   // + alignment slack
+    // chunk references of a pass, staged in shared memory after the ring
+    // when a chunk spans several stages (the chunk set-up then reads them
+    // from shared memory instead of waiting on global loads)
+    static_assert(sizeof(ChunkRef) == 48, "chunk reference record");
+    static constexpr bool CREF_SMEM = R > 1;
+    static constexpr int PASS_CHUNKS = kMaxPassStages / R + 1;
+    static constexpr size_t cref_bytes = CREF_SMEM ? PASS_CHUNKS * 48 : 0;
+    static constexpr size_t smem_bytes = NBUF * buf_bytes + cref_bytes + 128;   // + alignment slack
     static_assert(STAGE == 16 || STAGE == 32, "stage");
     static_assert(NBUF >= 2 && NBUF <= kMaxBuf, "ring");
     // tile-start lane keys and the prologue's stage geometry live at the
@@ -326,6 +333,13 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                 sh.wlo[q] = INT_MAX;
                 sh.whi[q] = INT_MIN;
             }
+            // the pass's chunk references (after the ring: no copy writes there)
+            const int ch0 = (cb * STAGE) / CHUNK;
+            ChunkRef *scref = reinterpret_cast<ChunkRef *>(smem + NBUF * Cfg::buf_bytes);
+            if (Cfg::CREF_SMEM) {
+                const int nch = ((cb + npass - 1) * STAGE) / CHUNK - ch0 + 1;
+                for (int k = t; k < nch; k += blockDim.x) scref[k] = ctab[ch0 + k];
+            }
             __syncthreads();
 #pragma unroll 2
             for (int q = 0; q < npass; ++q) {
@@ -411,9 +425,13 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                     if (gwork) {
                         ++chunks;
                         ChunkRef ref;
-                        ref.emax = __ldg(&ctab[chunk].emax);
-                        ref.thi = __ldg(&ctab[chunk].thi);
-                        ref.tlo = __ldg(&ctab[chunk].tlo);
+                        if (Cfg::CREF_SMEM) {
+                            ref = scref[chunk - ch0];
+                        } else {
+                            ref.emax = __ldg(&ctab[chunk].emax);
+                            ref.thi = __ldg(&ctab[chunk].thi);
+                            ref.tlo = __ldg(&ctab[chunk].tlo);
+                        }
                         chunk_setup(P, pf, ref, S);
                     } else {
                         safe_setup(S, 0);
