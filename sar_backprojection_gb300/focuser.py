@@ -16,7 +16,6 @@ checkpoint has nothing to resume (long scenes use ``large_scene``).
 from __future__ import annotations
 
 import ctypes as C
-import sys
 from dataclasses import dataclass
 
 import numpy as np
@@ -159,53 +158,72 @@ STREAM_BLOCKS = 8      # pulse blocks of a streamed drop-in upload
 # worst; the copy engine 3.91 ms mean, 3.35 ms median but 24 ms at the 99th
 # percentile and 75 ms worst (its host-to-device stalls)
 STREAM_UPLOAD = "sm"
-IMAGE_POOL = 4         # host images the drop-in call keeps for reuse
+FRESH_AHEAD = 2        # result arrays the drop-in call keeps faulted in ahead
 
 
-def _refs(a) -> int:
-    return sys.getrefcount(a)
-
-
-# references to an array held only by a list, counted as host_image counts them
-_POOL_ONLY_REFS = (lambda pool: _refs(pool[0]))([np.empty(1)])
-
-
-class HostImagePool:
+class FreshImages:
     """The complex128 (dim0, dim1) column-major host arrays the drop-in call
-    returns.
+    returns: each call gets a NEW array, as the reference's focusing call
+    returns one, whose pages a helper thread has already touched.  A fresh
+    16 MB result would otherwise cost thousands of page faults inside the
+    call.  The helper keeps up to FRESH_AHEAD arrays of the last shape asked
+    for; a call that finds none ready allocates one itself."""
 
-    An array of an earlier call that the caller no longer references (no
-    variable, view or tensor holds it: only this pool does) is reused, its
-    pages already mapped; otherwise a new one is made.  A fresh 16 MB result
-    costs thousands of page faults inside the call, and a caller that keeps
-    the previous result while making the next call would pay them on every
-    call.  The pool keeps at most IMAGE_POOL arrays; beyond that the oldest is
-    left to the caller alone.
-    """
+    def __init__(self, ahead: int = FRESH_AHEAD):
+        import threading
+        self.ahead = int(ahead)
+        self.ready: list = []                 # (shape, tensor) faulted in
+        self.shape = None
+        self.cv = threading.Condition()
+        self.thread = None
 
-    def __init__(self):
-        self.arrays: list[np.ndarray] = []
+    @staticmethod
+    def _make(dim0: int, dim1: int) -> torch.Tensor:
+        t = torch.empty((dim0 * dim1, 2), dtype=torch.float64)
+        t.zero_()                              # touches every page, interpreter lock released
+        return t
+
+    def _fill(self):
+        while True:
+            with self.cv:
+                while self.shape is None or len(self.ready) >= self.ahead:
+                    self.cv.wait()
+                shape = self.shape
+            t = self._make(*shape)
+            with self.cv:
+                if shape == self.shape and len(self.ready) < self.ahead:
+                    self.ready.append((shape, t))
 
     def get(self, dim0: int, dim1: int) -> np.ndarray:
-        for k in range(len(self.arrays)):
-            if (self.arrays[k].shape == (dim0, dim1)
-                    and _refs(self.arrays[k]) <= _POOL_ONLY_REFS):
-                return self.arrays[k]
-        a = np.empty((dim0, dim1), dtype=np.complex128, order="F")
-        self.arrays.append(a)
-        if len(self.arrays) > IMAGE_POOL:
-            self.arrays.pop(0)
-        return a
+        import threading
+        shape = (int(dim0), int(dim1))
+        t = None
+        with self.cv:
+            if self.shape != shape:
+                self.shape = shape
+                self.ready.clear()
+            if self.ready:
+                t = self.ready.pop()[1]
+            if self.thread is None:
+                self.thread = threading.Thread(target=self._fill, daemon=True)
+                self.thread.start()
+            self.cv.notify()
+        if t is None:
+            t = self._make(*shape)
+        # the array's memory is the tensor's; the array keeps it alive
+        flat = t.numpy().view(np.complex128).reshape(-1)
+        return np.reshape(flat, shape, order="F")
 
     def clear(self) -> None:
-        self.arrays.clear()
+        with self.cv:
+            self.ready.clear()
 
 
 class _DropIn:
     """Per-device resources the synchronous drop-in call reuses across calls:
     its copy and second compute stream, device buffers for the raw rows and
     the image (a caller's repeated calls then allocate nothing on the device)
-    and the pool of returned host images.  The lock serialises calls from
+    and the pre-faulted fresh host images it returns.  The lock serialises calls from
     several host threads."""
 
     def __init__(self, dev: torch.device):
@@ -216,7 +234,7 @@ class _DropIn:
         self.side = torch.cuda.Stream(dev)
         self.raw: dict[tuple, torch.Tensor] = {}
         self.out: dict[int, torch.Tensor] = {}
-        self.images = HostImagePool()
+        self.images = FreshImages()
 
     def raw_buffer(self, nra: int, naz: int, dev) -> torch.Tensor:
         key = (naz, nra + (nra & 1))

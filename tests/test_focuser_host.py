@@ -74,28 +74,25 @@ def test_flatten_matches_numpy_fortran_order():
                           m.astype(np.uint8).flatten(order="F"))
 
 
-def test_host_image_pool_reuses_only_unreferenced_arrays():
-    """The drop-in call's result arrays are reused only once nothing of the
-    caller's refers to them: a held array, a view of it or a tensor over it
-    keeps it out of reach of later calls."""
-    from sar_backprojection_gb300.focuser import IMAGE_POOL, HostImagePool
-    pool = HostImagePool()
+def test_drop_in_results_are_fresh_arrays():
+    """The drop-in call returns a new array every call, as the reference's
+    focusing call does (pages faulted in ahead by a helper thread): no
+    result shares memory with another, whether or not the caller holds it."""
+    import time
+    from sar_backprojection_gb300.focuser import FreshImages
+    pool = FreshImages(ahead=2)
     a = pool.get(4, 3)
     assert a.shape == (4, 3) and a.dtype == np.complex128 and a.flags.f_contiguous
+    time.sleep(0.05)                                 # let the helper fill ahead
     b = pool.get(4, 3)
-    assert b is not a                              # a is held by the caller
+    assert b is not a and not np.shares_memory(a, b)
+    a[...] = 1 + 2j
     del a
     c = pool.get(4, 3)
-    assert c is pool.arrays[0]                     # dropped: reused
-    view = c[1:]
-    t = torch.from_numpy(b.reshape(-1, order="F").view(np.float64))
-    d = pool.get(4, 3)
-    assert d is not c and d is not b
-    del view, t
-    assert pool.get(5, 3).shape == (5, 3)           # another shape: a new array
-    held = [pool.get(2, 2) for _ in range(IMAGE_POOL + 2)]
-    assert len({id(x) for x in held}) == len(held)
-    assert len(pool.arrays) <= IMAGE_POOL
+    assert not np.shares_memory(b, c) and (c == 0).all()
+    assert pool.get(5, 3).shape == (5, 3)           # another shape
+    held = [pool.get(2, 2) for _ in range(6)]
+    assert all(not np.shares_memory(x, y) for i, x in enumerate(held) for y in held[i + 1:])
 
 
 def test_scene_upload_mode_arguments_are_checked_before_the_device():
