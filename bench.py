@@ -292,10 +292,11 @@ def run_reference(args, dist: Dist):
         "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": DATA,
-        "config": {"workload": workload_name, "precision": "fp64 (reference semantics)",
-                   "implementation": "oracle C restatement of process_point/"
-                                     "FocalizzatoreBpPx, OpenMP over pixels",
-                   "l2": "host run (no GPU)"},
+        "config": {"workload": workload_name, "seed": args.seed},
+        "details": {"precision": "fp64 (reference semantics)",
+                    "implementation": "oracle C restatement of process_point/"
+                                      "FocalizzatoreBpPx, OpenMP over pixels",
+                    "l2": "host run (no GPU)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": sample, "reference_as_is": reference_timing()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -892,12 +893,11 @@ def run_ours(args, dist: Dist):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 per pulse; float-float (f32 pairs) per-chunk reference range and phase",
             "data": DATA,
-            "config": {"workload": workload_name, "precision": "mixed",
-                       "nominal_pixel_pulses_per_scene": work,
-                       "tuning": tuning.as_dict(),
-                       "autotune_ms": autotune,
-                       "l2": "inputs larger than L2 (1.52 GB raw data re-read every step)",
-                       "scenes": f"one per GPU (seed {args.seed}+rank)"},
+            "config": {"workload": workload_name, "seed": args.seed},
+            "details": {"precision": "mixed", "nominal_pixel_pulses_per_scene": work,
+                        "tuning": tuning.as_dict(), "autotune_ms": autotune,
+                        "l2": "inputs larger than L2 (1.52 GB raw data re-read every step)",
+                        "scenes": f"one per GPU (seed {args.seed}+rank)"},
             "fp64": ({"value": dist.world * work / (fp64_ms * 1e-3) / 1e9, "unit": UNIT,
                       "ms_per_step": fp64_ms, "steps": args.fp64_steps} if fp64_ms else None),
             "speedup_mixed_vs_fp64": fp64_ms / ms_per_step if fp64_ms else None,
