@@ -152,11 +152,12 @@ def FocalizzatoreBpPx(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
 
 STREAM_BLOCKS = 8      # pulse blocks of a streamed drop-in upload
 # how the streamed drop-in copies the reachable raw bins from page-locked
-# host memory: "sm" (SM loads on a high-priority stream, whose CTAs take SMs
-# as focusing CTAs finish) or "copy" (copy engine).  Measured over 450 calls
-# each on the full workload: SM loads 3.99 ms mean, 4.01 ms median, 4.19 ms
-# worst; the copy engine 3.91 ms mean, 3.35 ms median but 24 ms at the 99th
-# percentile and 75 ms worst (its host-to-device stalls)
+# host memory: "sm" (SM loads of 16-byte words, one CTA per SM, on a stream of
+# the highest priority, so its CTAs take SMs as focusing CTAs finish) or
+# "copy" (copy engine).  Measured over 240 calls each on the full workload:
+# SM loads 3.89 ms mean, 3.85 ms median, 4.09 ms at the 99th percentile; the
+# copy engine 4.17 ms mean, 3.41 ms median, 9.5 ms at the 99th percentile and
+# 86 ms worst (its host-to-device stalls)
 STREAM_UPLOAD = "sm"
 FRESH_AHEAD = 2        # result arrays the drop-in call keeps faulted in ahead
 

@@ -25,14 +25,22 @@ def _stream():
     return torch.cuda.current_stream().cuda_stream
 
 
-def test_raw_bins_match_the_copy_engine(lib):
-    naz, nra, lo, nb = 257, 1001, 123, 517          # odd pitch and offsets
+@pytest.mark.parametrize("naz,nra,dpitch,lo,nb", [
+    (257, 1001, 1002, 123, 517),     # odd source pitch: complex64 words
+    (257, 1000, 1000, 123, 517),     # even pitches, odd start and end: head and tail bins
+    (257, 1000, 1002, 122, 518),     # even start and end: pairs only
+    (257, 1000, 1000, 123, 518),     # odd start, even end
+    (64, 4762, 4762, 209, 1577),     # the full workload's reachable bins
+    (3, 8, 8, 1, 1),                 # one bin, odd: head only
+    (3, 8, 8, 2, 1),                 # one bin, even: tail only
+])
+def test_raw_bins_match_the_copy_engine(lib, naz, nra, dpitch, lo, nb):
     host = torch.randn((naz, nra, 2), dtype=torch.float32).pin_memory()
-    a = torch.full((naz, nra + 1, 2), 7.0, device="cuda")
+    a = torch.full((naz, dpitch, 2), 7.0, device="cuda")
     b = a.clone()
-    _lib.check(lib.sarbp_upload_raw_bins(a.data_ptr(), nra + 1, host.data_ptr(), nra, lo, nb,
+    _lib.check(lib.sarbp_upload_raw_bins(a.data_ptr(), dpitch, host.data_ptr(), nra, lo, nb,
                                          naz, _stream()))
-    _lib.check(lib.sarbp_upload_raw_bins_sm(b.data_ptr(), nra + 1, host.data_ptr(), nra, lo, nb,
+    _lib.check(lib.sarbp_upload_raw_bins_sm(b.data_ptr(), dpitch, host.data_ptr(), nra, lo, nb,
                                             naz, _stream()))
     torch.cuda.synchronize()
     assert torch.equal(a, b)
