@@ -63,9 +63,7 @@ gather_rows_kernel(float2 *__restrict__ dst, int64_t dpitch, const float2 *__res
 // pitches and 16-byte aligned buffers: bins [lo, lo + n) split into an odd
 // head bin, a body of whole pairs and an odd tail bin, so exactly those bins
 // are written.  Half the load instructions for the same bytes in flight.
-// One CTA per SM: the drop-in call's uploads share the SMs with focusing
-// CTAs, and fewer, longer-lived copy CTAs measured 4 % faster calls than
-// two per SM (3.89 vs 4.07 ms on the full workload; 64 CTAs the same).
+
 __global__ void __launch_bounds__(kCopyThreads)
 gather_rows16_kernel(float2 *__restrict__ dst, int64_t dpitch, const float2 *__restrict__ src,
                      int64_t spitch, int64_t lo, int64_t n, int64_t rows)
@@ -121,28 +119,33 @@ copy_bytes_kernel(unsigned char *__restrict__ dst, const unsigned char *__restri
     for (int64_t i = tail + tid; i < bytes; i += stride) dst[i] = src[i];
 }
 
-static int row_grid(int64_t rows)
+// CTAs of a row copy: `per_sm` per SM, at most one per row.  An upload that
+// shares the SMs with focusing CTAs (the drop-in call) runs best with one
+// per SM: fewer, longer-lived copy CTAs measured 4 % faster calls than two
+// per SM (3.89 vs 4.07 ms on the full workload; 64 CTAs the same); on an
+// otherwise idle GPU (the serving queue) more CTAs keep more loads in flight.
+static int row_grid(int64_t rows, int per_sm)
 {
     int dev = 0, sms = 148;
     if (cudaGetDevice(&dev) == cudaSuccess)
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t g = sms;
+    const int64_t g = (int64_t)per_sm * sms;
     return (int)(rows < g ? (rows > 0 ? rows : 1) : g);
 }
 
 // Rows [0, rows) of bins [lo, lo + n): 16-byte words where pitches and
 // buffers allow, complex64 words otherwise.
 static void launch_rows(float2 *dst, int64_t dpitch, const float2 *sv, int64_t spitch,
-                        int64_t lo, int64_t n, int64_t rows, cudaStream_t stream)
+                        int64_t lo, int64_t n, int64_t rows, int per_sm, cudaStream_t stream)
 {
     const bool vec = !(dpitch & 1) && !(spitch & 1) &&
                      !(reinterpret_cast<uintptr_t>(dst) & 15) &&
                      !(reinterpret_cast<uintptr_t>(sv) & 15);
     if (vec)
-        gather_rows16_kernel<<<row_grid(rows), kCopyThreads, 0, stream>>>(dst, dpitch, sv,
+        gather_rows16_kernel<<<row_grid(rows, per_sm), kCopyThreads, 0, stream>>>(dst, dpitch, sv,
                                                                         spitch, lo, n, rows);
     else
-        gather_rows_kernel<<<row_grid(rows), kCopyThreads, 0, stream>>>(dst, dpitch, sv, spitch,
+        gather_rows_kernel<<<row_grid(rows, per_sm), kCopyThreads, 0, stream>>>(dst, dpitch, sv, spitch,
                                                                       lo, n, rows);
 }
 
@@ -204,7 +207,8 @@ int h2d_rows(float2 *dst, int64_t dpitch, const float2 *src, int64_t spitch, int
 {
     if (n <= 0 || rows <= 0) return SARBP_OK;
     if (const void *sv = device_view(src)) {
-        launch_rows(dst, dpitch, static_cast<const float2 *>(sv), spitch, lo, n, rows, stream);
+        launch_rows(dst, dpitch, static_cast<const float2 *>(sv), spitch, lo, n, rows, 4,
+                    stream);
         return cuda_status(cudaGetLastError(), "raw rows copy (SM loads)");
     }
     return cuda_status(cudaMemcpy2DAsync(dst + lo, (size_t)dpitch * sizeof(float2), src + lo,
@@ -238,7 +242,7 @@ extern "C" SARBP_API int sarbp_upload_raw_bins_sm(void *dst, int64_t dst_pitch, 
         return SARBP_EINVAL;
     }
     launch_rows(static_cast<float2 *>(dst), dst_pitch, static_cast<const float2 *>(sv), src_pitch,
-                bin_lo, nbins, npulses, static_cast<cudaStream_t>(stream));
+                bin_lo, nbins, npulses, 1, static_cast<cudaStream_t>(stream));
     return cuda_status(cudaGetLastError(), "sarbp_upload_raw_bins_sm launch");
 }
 
