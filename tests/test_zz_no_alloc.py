@@ -84,6 +84,43 @@ def test_noalloc_reports_a_wait_that_runs_out():
     assert int(ctr[_lib.CTR_TIMEOUTS].item()) == 0
 
 
+def test_noalloc_queue_that_does_not_fit_falls_back_to_one_cta_per_tile():
+    """A staged=2 tuning on a scene whose chunk tables fit the built-in
+    scratch but whose tile queue (62,500 tiles) does not: the call runs one
+    CTA per tile instead and still gives the workspace entry point's image."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.set_device(0)
+    dim0, dim1, naz, nra = 4000, 2000, 131072, 64
+    dev = torch.device("cuda", 0)
+    k = torch.arange(naz, dtype=torch.float64)
+    tx, ty, tz = 0.5 * k, torch.full((naz,), -2000.0, dtype=torch.float64), \
+        torch.full((naz,), 3000.0, dtype=torch.float64)
+    xs = 16.0 * torch.arange(dim0, dtype=torch.float64) + 8.0
+    ys = 100.0 + 0.01 * torch.arange(dim1, dtype=torch.float64)
+    x = xs[:, None].expand(dim0, dim1)
+    y = ys[None, :].expand(dim0, dim1)
+    z = torch.zeros(dim0, dim1, dtype=torch.float64)
+    near = float(torch.sqrt(torch.tensor(2100.0 ** 2 + 3000.0 ** 2))) - 4.0
+    index = torch.round(x / 0.5).to(torch.int32)
+    sint = torch.full((dim0, dim1), 7, dtype=torch.int32)
+    mask = torch.ones(dim0, dim1, dtype=torch.uint8)
+    g = torch.Generator().manual_seed(5)
+    raw = torch.complex(torch.randn(naz, nra, generator=g),
+                        torch.randn(naz, nra, generator=g)).to(torch.complex64).t()
+    ds = scene_to_device(x.numpy(), y.numpy(), z.numpy(), mask.numpy(), index.numpy(),
+                         tx.numpy(), ty.numpy(), tz.numpy(), raw, near, 0.5, 0.031,
+                         sint.numpy(), device=dev)
+    queued = dict(chunk=64, tile0=16, tile1=8, staged=2, window=128)
+    ref = focus(ds, "mixed", tuning=dict(queued, staged=1), diagnostics=True).check()
+    torch.cuda.synchronize()
+    rc, out, nv, cs, ctr = _noalloc(ds, queued)
+    _lib.check(rc)
+    assert torch.equal(out, ref.image) and torch.equal(nv, ref.nvalid)
+    assert torch.equal(cs, ref.checksum)
+    assert int(nv.max().item()) > 0
+
+
 def test_noalloc_rejects_scenes_beyond_its_limit():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
