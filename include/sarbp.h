@@ -40,6 +40,7 @@ extern "C" {
 #define SARBP_ETIMEOUT     -4   /* a bounded device wait gave up */
 #define SARBP_ERANGE       -5   /* size beyond a documented limit */
 #define SARBP_EDEVICE      -6   /* device is not a GB300-class sm_103 GPU */
+#define SARBP_ECANCELED    -7   /* a serving-queue job was cancelled before admission */
 
 /*
  * One focusing scene: the reference's 13 positional arguments
@@ -397,6 +398,14 @@ SARBP_API int64_t sarbp_queue_completed(sarbp_queue *queue, int64_t *ids, double
  * and device -> host for host jobs.  No reference counterpart.
  */
 SARBP_API int sarbp_queue_stats(sarbp_queue *queue, int64_t *stats);
+/*
+ * Cancel a job that is still waiting for admission: it is reported done with
+ * status SARBP_ECANCELED (through sarbp_queue_completed, _poll or _wait) and
+ * none of its buffers is touched.  SARBP_EINVAL for a job that is already
+ * admitted (its work is on the device) or unknown.  No reference
+ * counterpart.
+ */
+SARBP_API int sarbp_queue_cancel(sarbp_queue *queue, int64_t job);
 
 /*
  * 8-bit amplitude preview of a focused image: out[i] = clip(|image[i]| *

@@ -17,6 +17,7 @@ SARBP_ECUDA = -3
 SARBP_ETIMEOUT = -4
 SARBP_ERANGE = -5
 SARBP_EDEVICE = -6
+SARBP_ECANCELED = -7
 
 CTR_AMBIGUOUS = 0
 CTR_WINDOW_MISS = 1
@@ -87,6 +88,7 @@ SIGNATURES = {
     "sarbp_queue_job_bytes": (C.c_int64, [_P, C.POINTER(Scene)]),
     "sarbp_queue_submit_host": (C.c_int64, [_P, C.POINTER(Scene), _P]),
     "sarbp_queue_stats": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "sarbp_queue_cancel": (C.c_int, [_P, C.c_int64]),
     "sarbp_queue_completed": (C.c_int64, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_double),
                                           C.POINTER(C.c_int32), C.c_int64]),
     "sarbp_tile_queue_keys": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, C.c_size_t,

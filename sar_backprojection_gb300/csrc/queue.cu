@@ -732,6 +732,33 @@ SARBP_API int64_t sarbp_queue_submit_host(sarbp_queue *queue, const sarbp_scene 
     return id;
 }
 
+SARBP_API int sarbp_queue_cancel(sarbp_queue *queue, int64_t job)
+{
+    if (!queue) {
+        set_error("sarbp_queue_cancel: queue is NULL");
+        return SARBP_EINVAL;
+    }
+    Queue &q = queue->q;
+    std::lock_guard<std::mutex> lk(q.mu);
+    auto it = q.jobs.find(job);
+    if (it == q.jobs.end()) {
+        set_error("sarbp_queue_cancel: unknown job %lld", (long long)job);
+        return SARBP_EINVAL;
+    }
+    auto pit = std::find(q.pending.begin(), q.pending.end(), job);
+    if (pit == q.pending.end()) {
+        set_error("sarbp_queue_cancel: job %lld is already admitted or done", (long long)job);
+        return SARBP_EINVAL;
+    }
+    q.pending.erase(pit);
+    QJob &j = *it->second;
+    j.status = SARBP_ECANCELED;
+    j.arena_bytes = 0;                 // nothing was carved for it
+    q.finish(j);
+    q.done_cv.notify_all();
+    return SARBP_OK;
+}
+
 SARBP_API int sarbp_queue_stats(sarbp_queue *queue, int64_t *stats)
 {
     if (!queue || !stats) {

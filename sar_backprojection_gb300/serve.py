@@ -448,6 +448,11 @@ class NativeQueue:
         done = _lib.check(int(self.lib.sarbp_queue_poll(self._q, job))) == 1
         return done
 
+    def cancel(self, job: int) -> None:
+        """Cancel a job still waiting for admission (SarbpError if it is
+        already admitted); waiting on it then raises with SARBP_ECANCELED."""
+        _lib.check(int(self.lib.sarbp_queue_cancel(self._q, job)))
+
     def wait(self, job: int) -> torch.Tensor:
         """Block until the job is done; its (npix, 2) float64 device image."""
         try:

@@ -179,3 +179,5 @@ def test_new_entry_points_reject_bad_arguments_without_a_gpu():
     assert lib.sarbp_queue_submit_host(None, C.byref(s), out) == _lib.SARBP_EINVAL
     ids = (C.c_int64 * 4)()
     assert lib.sarbp_queue_completed(None, ids, None, None, 4) == _lib.SARBP_EINVAL
+    assert lib.sarbp_queue_cancel(None, 0) == _lib.SARBP_EINVAL
+    assert lib.sarbp_queue_stats(None, ids) == _lib.SARBP_EINVAL

@@ -38,3 +38,24 @@ def test_queue_poll_reports_once(scenes):
         q.wait(j)
         with pytest.raises(Exception):
             q.poll(j)                                     # id released after completion
+
+
+def test_queue_cancels_a_waiting_job(scenes):
+    """With one scene slot, a job behind two others is still waiting when it
+    is cancelled: it reports SARBP_ECANCELED and the others still finish."""
+    from sar_backprojection_gb300 import _lib
+    with NativeQueue(max_slots=1) as q:
+        a = q.submit(scenes[3])                  # the largest scene first
+        b = q.submit(scenes[0])
+        c = q.submit(scenes[1])
+        q.cancel(c)
+        with pytest.raises(_lib.SarbpError) as e:
+            q.wait(c)
+        assert e.value.status == _lib.SARBP_ECANCELED
+        for j, ds in ((a, scenes[3]), (b, scenes[0])):
+            img = q.wait(j)
+            ref = focus(ds, "mixed", tuning=q.tuning).check()
+            torch.cuda.synchronize()
+            assert torch.equal(img, ref.image)
+        with pytest.raises(_lib.SarbpError):
+            q.cancel(a)                           # done and released

@@ -102,6 +102,23 @@ def test_native_engine_each_job_same_alone_and_in_the_mix(jobs, memory):
         assert np.array_equal(_bits(j.image), _bits(_alone(ref, tuning))), f"job {j.job_id}"
 
 
+def test_native_engine_images_meet_the_bars_against_the_oracle(jobs):
+    """Served images checked against the oracle directly (not only through
+    the single-scene kernel): coherence >= 0.9999, RMS phase <= 1 mrad,
+    rel-L2 <= 1e-3, and zero exactly where the oracle has no contributor."""
+    from oracle import oracle
+    from sar_backprojection_gb300 import quality
+    mine = [serve.Job(job_id=j.job_id, arrival=j.arrival, args=j.args) for j in jobs[:6]]
+    with serve.NativeServingEngine(budget_bytes=4 * serve.GB, max_slots=4) as eng:
+        eng.run(mine)
+    for j in mine:
+        ref, nv, _ = oracle.focus(*j.args)
+        q = quality.compare(j.image, ref)
+        assert q["coherence"] >= 0.9999 and q["rms_phase_mrad"] <= 1.0, (j.job_id, q)
+        assert q["rel_l2"] <= 1e-3, (j.job_id, q)
+        assert (j.image[nv == 0] == 0).all()
+
+
 def test_native_engine_reserved_memory_limits_residency(jobs):
     """A reserve that holds one job at a time still completes every job; a
     job larger than the whole reserve is refused at submission."""
