@@ -21,8 +21,9 @@ Printed (rank 0, one JSON line):
   cpu_baseline  the oracle's C restatement on the host cores, bounded sample
 
 ``--impl reference`` times the reference algorithm's CPU implementation (the
-oracle port: the reference is Python + Numba and its own code cannot run on
-the GPU machine) on all host cores over a bounded pixel sample per step.
+oracle port: the reference is Python + Numba, and its own code is not
+shipped with this package) on all host cores over a bounded pixel sample per
+step.
 """
 from __future__ import annotations
 
@@ -239,7 +240,7 @@ def reference_timing() -> dict | None:
     """The reference's own focusing call timed where its source is available
     (tests/golden/reference_timing.json, written by tests/golden/make_golden.py):
     one core, NumPy interpreting the Numba-decorated loop (no Numba there), on
-    the build container's CPU, not this host."""
+    the CPU of the machine that generated the fixtures, not this host."""
     path = Path(__file__).resolve().parent / "tests" / "golden" / "reference_timing.json"
     try:
         t = json.loads(path.read_text())
@@ -247,8 +248,8 @@ def reference_timing() -> dict | None:
         return None
     t["unit"] = UNIT
     t["value"] = t.pop("gpix_pulse_per_s")
-    t["note"] = ("measured in the build container, not on this host; Numba's JIT is absent "
-                 "there, so the loop runs as plain NumPy")
+    t["note"] = ("measured on the machine that generated the fixtures, not on this host; "
+                 "Numba's JIT is absent there, so the loop runs as plain NumPy")
     return t
 
 
