@@ -265,6 +265,28 @@ SARBP_API int sarbp_upload_raw_bins_sm(void *dst, int64_t dst_pitch, const void 
 SARBP_API int sarbp_copy_to_device_sm(void *dst, const void *src, int64_t bytes, void *stream);
 
 /*
+ * The same rows in pulse blocks, copied by one persistent grid of `ctas`
+ * CTAs that signals each block: block k is rows [block_ends[k-1],
+ * block_ends[k]) (block_ends non-decreasing, at most 32 blocks); when every
+ * CTA has copied its share of block k, flags[k] (device uint32) is set to
+ * `generation` (non-zero; use a new value per call, e.g. a counter, since
+ * flags are never cleared).  counters (device uint32[nblocks]) is scratch,
+ * cleared by the call in stream order.  sarbp_stream_wait_flag holds a
+ * stream until a flag has reached a value (cuStreamWaitValue32, greater or
+ * equal in wrap-around order): work that needs block k is queued behind
+ * flags[k] and starts while later blocks are still being copied, and the
+ * copy occupies only `ctas` SMs.  Source as for sarbp_upload_raw_bins_sm,
+ * 16-byte aligned; both pitches even; the destination 16-byte aligned.
+ * No reference counterpart.
+ */
+SARBP_API int sarbp_upload_raw_blocks_sm(void *dst, int64_t dst_pitch, const void *src,
+                                         int64_t src_pitch, int64_t bin_lo, int64_t nbins,
+                                         const int64_t *block_ends, int32_t nblocks,
+                                         uint32_t *flags, uint32_t *counters,
+                                         uint32_t generation, int32_t ctas, void *stream);
+SARBP_API int sarbp_stream_wait_flag(void *stream, const uint32_t *flag, uint32_t value);
+
+/*
  * Batches: many scenes of uneven size in one persistent launch.
  * Replaces the reference's per-batch host loops (gpu_small_dataset.py:285-339,
  * main_gpu.py:415-586), which launch one kernel per pixel batch and copy

@@ -95,6 +95,68 @@ gather_rows16_kernel(float2 *__restrict__ dst, int64_t dpitch, const float2 *__r
     }
 }
 
+// Pulse blocks of rows copied by a persistent grid that signals each block:
+// block k holds rows [ends[k-1], ends[k]); every CTA copies its share of a
+// block's rows, then counts itself done with the block; the last CTA to do
+// so stores `generation` into flags[k].  A stream can then be held until
+// flags[k] >= generation (sarbp_stream_wait_flag), so work on block k starts
+// while later blocks are still being copied, and no kernel waits on
+// another.  The copy runs on a few SMs only, leaving the rest to the work
+// it feeds.
+constexpr int kMaxBlocks = 32;
+struct BlockEnds {
+    int64_t end[kMaxBlocks];
+};
+
+__device__ __forceinline__ void copy_row16(float2 *__restrict__ drow, const float2 *__restrict__ srow,
+                                           int64_t lo, int64_t lo_up, int64_t hi, int64_t n2)
+{
+    if (threadIdx.x == 0) {
+        if (lo & 1) drow[lo] = srow[lo];
+        if ((hi & 1) && hi - 1 >= lo_up) drow[hi - 1] = srow[hi - 1];
+    }
+    const uint4 *s = reinterpret_cast<const uint4 *>(srow + lo_up);
+    uint4 *d = reinterpret_cast<uint4 *>(drow + lo_up);
+    for (int64_t i = threadIdx.x; i < n2; i += (int64_t)kCopyUnroll * kCopyThreads) {
+        uint4 v[kCopyUnroll];
+#pragma unroll
+        for (int u = 0; u < kCopyUnroll; ++u) {
+            const int64_t k = i + (int64_t)u * kCopyThreads;
+            if (k < n2) v[u] = s[k];
+        }
+#pragma unroll
+        for (int u = 0; u < kCopyUnroll; ++u) {
+            const int64_t k = i + (int64_t)u * kCopyThreads;
+            if (k < n2) d[k] = v[u];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kCopyThreads)
+gather_blocks16_kernel(float2 *__restrict__ dst, int64_t dpitch, const float2 *__restrict__ src,
+                       int64_t spitch, int64_t lo, int64_t n, const BlockEnds ends, int nblocks,
+                       unsigned *__restrict__ counters, unsigned *__restrict__ flags,
+                       unsigned generation)
+{
+    const int64_t lo_up = (lo + 1) & ~int64_t(1), hi = lo + n, hi_dn = hi & ~int64_t(1);
+    const int64_t n2 = hi_dn > lo_up ? (hi_dn - lo_up) / 2 : 0;
+    int64_t a0 = 0;
+    for (int k = 0; k < nblocks; ++k) {
+        const int64_t a1 = ends.end[k];
+        for (int64_t r = a0 + blockIdx.x; r < a1; r += gridDim.x)
+            copy_row16(dst + r * dpitch, src + r * spitch, lo, lo_up, hi, n2);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();                      // this CTA's rows before its count
+            if (atomicAdd(&counters[k], 1u) == gridDim.x - 1) {
+                __threadfence();
+                atomicExch(&flags[k], generation);
+            }
+        }
+        a0 = a1;
+    }
+}
+
 // Byte copy: 16-byte words when both ends share their alignment mod 16, the
 // unaligned head and the tail byte by byte.
 __global__ void __launch_bounds__(kCopyThreads)
@@ -262,4 +324,86 @@ extern "C" SARBP_API int sarbp_copy_to_device_sm(void *dst, const void *src, int
     }
     launch_copy_bytes(dst, sv, bytes, static_cast<cudaStream_t>(stream));
     return cuda_status(cudaGetLastError(), "sarbp_copy_to_device_sm launch");
+}
+
+extern "C" SARBP_API int sarbp_upload_raw_blocks_sm(void *dst, int64_t dst_pitch, const void *src,
+                                                   int64_t src_pitch, int64_t bin_lo,
+                                                   int64_t nbins, const int64_t *block_ends,
+                                                   int32_t nblocks, uint32_t *flags,
+                                                   uint32_t *counters, uint32_t generation,
+                                                   int32_t ctas, void *stream)
+{
+    if (!dst || !src || !block_ends || !flags || !counters || dst_pitch <= 0 || src_pitch <= 0 ||
+        bin_lo < 0 || nbins <= 0 || bin_lo + nbins > dst_pitch || bin_lo + nbins > src_pitch ||
+        nblocks <= 0 || nblocks > kMaxBlocks || ctas <= 0 || generation == 0 ||
+        (dst_pitch & 1) || (src_pitch & 1) || (reinterpret_cast<uintptr_t>(dst) & 15)) {
+        set_error("sarbp_upload_raw_blocks_sm: bad pointers, bin range [%lld, +%lld), pitches "
+                  "%lld / %lld (both even), %d blocks (1..%d), %d CTAs or generation 0",
+                  (long long)bin_lo, (long long)nbins, (long long)dst_pitch,
+                  (long long)src_pitch, nblocks, kMaxBlocks, ctas);
+        return SARBP_EINVAL;
+    }
+    BlockEnds e{};
+    int64_t prev = 0;
+    for (int k = 0; k < nblocks; ++k) {
+        if (block_ends[k] < prev) {
+            set_error("sarbp_upload_raw_blocks_sm: block ends must not decrease");
+            return SARBP_EINVAL;
+        }
+        e.end[k] = prev = block_ends[k];
+    }
+    const void *sv = device_view(src);
+    if (!sv || (reinterpret_cast<uintptr_t>(sv) & 15)) {
+        set_error("sarbp_upload_raw_blocks_sm: the source is not 16-byte aligned page-locked "
+                  "host memory mapped into the device's address space (or device memory)");
+        return SARBP_EINVAL;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int rc = cuda_status(cudaMemsetAsync(counters, 0, sizeof(uint32_t) * nblocks, s),
+                         "sarbp_upload_raw_blocks_sm: counters");
+    if (rc) return rc;
+    gather_blocks16_kernel<<<ctas, kCopyThreads, 0, s>>>(
+        static_cast<float2 *>(dst), dst_pitch, static_cast<const float2 *>(sv), src_pitch, bin_lo,
+        nbins, e, nblocks, counters, flags, generation);
+    return cuda_status(cudaGetLastError(), "sarbp_upload_raw_blocks_sm launch");
+}
+
+namespace {
+using WaitValueFn = int (*)(void *stream, unsigned long long addr, unsigned value, unsigned flags);
+
+WaitValueFn wait_value_fn()
+{
+    static WaitValueFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuStreamWaitValue32", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<WaitValueFn>(p);
+    }
+    return fn;
+}
+}  // namespace
+
+extern "C" SARBP_API int sarbp_stream_wait_flag(void *stream, const uint32_t *flag, uint32_t value)
+{
+    if (!flag) {
+        set_error("sarbp_stream_wait_flag: flag is NULL");
+        return SARBP_EINVAL;
+    }
+    auto fn = wait_value_fn();
+    if (!fn) {
+        set_error("sarbp_stream_wait_flag: cuStreamWaitValue32 is unavailable");
+        return SARBP_ECUDA;
+    }
+    const unsigned kWaitGeq = 0x0;   // CU_STREAM_WAIT_VALUE_GEQ
+    const int r = fn(stream, reinterpret_cast<unsigned long long>(flag), value, kWaitGeq);
+    if (r != 0) {
+        set_error("sarbp_stream_wait_flag: cuStreamWaitValue32 failed (CUresult %d)", r);
+        return SARBP_ECUDA;
+    }
+    return SARBP_OK;
 }

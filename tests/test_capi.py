@@ -138,6 +138,21 @@ def test_new_entry_points_reject_bad_arguments_without_a_gpu():
                                        None) == _lib.SARBP_EINVAL
     assert lib.sarbp_copy_to_device_sm(C.c_void_p(0x1000), C.c_void_p(0x2000), 0,
                                        None) == _lib.SARBP_OK
+    # block-signalled copy: odd pitch, decreasing ends, too many blocks, generation 0
+    ends = (C.c_int64 * 40)(*range(1, 41))
+    fl, ct = C.c_void_p(0x5000), C.c_void_p(0x6000)
+    args = [C.c_void_p(0x1000), 100, C.c_void_p(0x2000), 100, 0, 10, ends, 4, fl, ct, 1, 8,
+            None]
+    for i, bad in ((1, 101), (3, 99), (5, 101), (7, 33), (7, 0), (10, 0), (11, 0), (0, None)):
+        a = list(args)
+        a[i] = bad
+        assert lib.sarbp_upload_raw_blocks_sm(*a) == _lib.SARBP_EINVAL, (i, bad)
+    desc = (C.c_int64 * 3)(5, 3, 9)
+    a = list(args)
+    a[6], a[7] = desc, 3
+    assert lib.sarbp_upload_raw_blocks_sm(*a) == _lib.SARBP_EINVAL
+    assert "decrease" in _lib.last_error()
+    assert lib.sarbp_stream_wait_flag(None, None, 1) == _lib.SARBP_EINVAL
     s = _lib.Scene()
     s.dim0, s.dim1 = 64, 16
     for f in ("dem_x", "dem_y", "dem_z", "mask", "index", "sint", "traj_x", "traj_y",

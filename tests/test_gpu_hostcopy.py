@@ -63,6 +63,40 @@ def test_bytes_match(lib, offset, size):
         assert int(got[:dofs].sum()) == 0 and int(got[dofs + size:].sum()) == 0
 
 
+@pytest.mark.parametrize("naz,nra,dpitch,lo,nb,ends,ctas", [
+    (257, 1000, 1002, 123, 517, [40, 41, 41, 200, 257], 7),   # an empty block
+    (64, 4762, 4762, 209, 1577, [8 * k for k in range(1, 9)], 32),
+    (5, 8, 8, 1, 1, [5], 64),                                  # more CTAs than rows
+])
+def test_signalled_blocks_match_the_copy_engine(lib, naz, nra, dpitch, lo, nb, ends, ctas):
+    """The persistent block copy writes the copy engine's bytes, and after it
+    every block's flag holds the call's generation; a stream held behind the
+    last flag sees every row."""
+    host = torch.randn((naz, nra, 2), dtype=torch.float32).pin_memory()
+    a = torch.full((naz, dpitch, 2), 7.0, device="cuda")
+    b = a.clone()
+    flags = torch.zeros(32, dtype=torch.int32, device="cuda")
+    counters = torch.zeros(32, dtype=torch.int32, device="cuda")
+    e = np.asarray(ends, dtype=np.int64)
+    _lib.check(lib.sarbp_upload_raw_bins(a.data_ptr(), dpitch, host.data_ptr(), nra, lo, nb,
+                                         naz, _stream()))
+    for gen in (1, 2):
+        copy = torch.cuda.Stream()
+        copy.wait_stream(torch.cuda.current_stream())
+        _lib.check(lib.sarbp_upload_raw_blocks_sm(
+            b.data_ptr(), dpitch, host.data_ptr(), nra, lo, nb, e.ctypes.data, len(ends),
+            flags.data_ptr(), counters.data_ptr(), gen, ctas, copy.cuda_stream))
+        user = torch.cuda.Stream()
+        _lib.check(lib.sarbp_stream_wait_flag(user.cuda_stream,
+                                              flags.data_ptr() + 4 * (len(ends) - 1), gen))
+        with torch.cuda.stream(user):
+            seen = b.clone()
+        torch.cuda.synchronize()
+        assert torch.equal(seen, a)
+        assert flags[:len(ends)].tolist() == [gen] * len(ends)
+        assert counters[:len(ends)].tolist() == [ctas] * len(ends)
+
+
 def test_pageable_source_is_rejected(lib):
     src = np.zeros(4096, dtype=np.uint8)                 # not page-locked
     dst = torch.zeros(4096, dtype=torch.uint8, device="cuda")
@@ -71,6 +105,12 @@ def test_pageable_source_is_rejected(lib):
     rc = lib.sarbp_upload_raw_bins_sm(dst.data_ptr(), 64, src.ctypes.data, 64, 0, 8, 8,
                                       _stream())
     assert rc == _lib.SARBP_EINVAL
+    ends = np.asarray([8], dtype=np.int64)
+    flags = torch.zeros(2, dtype=torch.int32, device="cuda")
+    rc = lib.sarbp_upload_raw_blocks_sm(dst.data_ptr(), 64, src.ctypes.data, 64, 0, 8,
+                                        ends.ctypes.data, 1, flags.data_ptr(),
+                                        flags.data_ptr() + 4, 1, 4, _stream())
+    assert rc == _lib.SARBP_EINVAL and "page-locked" in _lib.last_error()
 
 
 def _pinned_args(sc):

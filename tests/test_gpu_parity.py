@@ -234,20 +234,25 @@ def test_full_workload_production_launch(full_scene, full_oracle, tuning):
                                                           "rms_phase_mrad")})
 
 
-def test_full_workload_streamed_drop_in(full_scene, full_oracle):
+@pytest.mark.parametrize("upload", ["sm", "signal", "copy"])
+def test_full_workload_streamed_drop_in(full_scene, full_oracle, upload, monkeypatch):
     """The drop-in call as the bench's e2e measures it: host inputs in the
     reference's layout, precision="mixed" with the bench's preferred tuning,
-    the reachable range bins streamed up in pulse blocks while focusing runs.
-    The returned image must equal the resident launch of the same tuning bit
-    for bit (whose range bins equal the oracle's) and meet the bars against
-    the oracle."""
+    the reachable range bins streamed up in pulse blocks while focusing runs
+    (by each upload mode: SM loads per block, one persistent block copy that
+    signals each block through a device flag, the copy engine).  The
+    returned image must equal the resident launch of the same tuning bit for
+    bit (whose range bins equal the oracle's) and meet the bars against the
+    oracle."""
     from sar_backprojection_gb300 import FocalizzatoreBpPx, focuser
 
+    monkeypatch.setattr(focuser, "STREAM_UPLOAD", upload)
     oimg, onv, ocs = full_oracle
     tuning = _bench_tunings()[0]
     host = dict(full_scene)
     host["RawData"] = full_scene["RawData"].cpu()       # (nra, naz), pulse-major memory
-    img = FocalizzatoreBpPx(*synth.focus_args(host), precision="mixed", tuning=tuning)
+    for _ in range(2):                                   # second call: next flag generation
+        img = FocalizzatoreBpPx(*synth.focus_args(host), precision="mixed", tuning=tuning)
     assert focuser.last_call["streamed"]
     assert img.shape == (4000, 250) and img.dtype == np.complex128
     ds = scene_to_device(*synth.focus_args(full_scene))
