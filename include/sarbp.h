@@ -265,6 +265,17 @@ SARBP_API int sarbp_upload_raw_bins_sm(void *dst, int64_t dst_pitch, const void 
 SARBP_API int sarbp_copy_to_device_sm(void *dst, const void *src, int64_t bytes, void *stream);
 
 /*
+ * n host-to-device copies in one call: bytes[i] bytes from src[i] (host) to
+ * dst[i] (device), by SM loads where the source is page-locked, else by the
+ * copy engine (cudaMemcpyAsync; a pageable source is staged by the driver
+ * before the call returns).  All arguments are checked before the first
+ * copy.  Used by the drop-in call for the DEM, masks and trajectory (nine
+ * arrays, one foreign call).  No reference counterpart.
+ */
+SARBP_API int sarbp_upload_host_arrays(int32_t n, void *const *dst, const void *const *src,
+                                       const int64_t *bytes, void *stream);
+
+/*
  * The same rows in pulse blocks, copied by one persistent grid of `ctas`
  * CTAs that signals each block: block k is rows [block_ends[k-1],
  * block_ends[k]) (block_ends non-decreasing, at most 32 blocks); when every
@@ -284,6 +295,17 @@ SARBP_API int sarbp_upload_raw_blocks_sm(void *dst, int64_t dst_pitch, const voi
                                          const int64_t *block_ends, int32_t nblocks,
                                          uint32_t *flags, uint32_t *counters,
                                          uint32_t generation, int32_t ctas, void *stream);
+/* The same, with the bin interval read by the copy kernel from `bound`
+ * (int32[2], inclusive, as sarbp_raw_bin_range_async leaves it: empty when
+ * bound[0] > bound[1]; clipped to the rows), device memory or page-locked
+ * host memory written in stream order before the copy starts: the copy can
+ * be queued behind the bound's computation without the host waiting for it.
+ * Every flag is still set when the interval is empty. */
+SARBP_API int sarbp_upload_raw_blocks_bound_sm(void *dst, int64_t dst_pitch, const void *src,
+                                               int64_t src_pitch, const int32_t *bound,
+                                               const int64_t *block_ends, int32_t nblocks,
+                                               uint32_t *flags, uint32_t *counters,
+                                               uint32_t generation, int32_t ctas, void *stream);
 SARBP_API int sarbp_stream_wait_flag(void *stream, const uint32_t *flag, uint32_t value);
 
 /*

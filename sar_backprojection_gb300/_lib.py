@@ -106,7 +106,11 @@ SIGNATURES = {
     "sarbp_copy_to_device_sm": (C.c_int, [_P, _P, C.c_int64, _P]),
     "sarbp_upload_raw_blocks_sm": (C.c_int, [_P, C.c_int64, _P, C.c_int64, C.c_int64, C.c_int64,
                                              _P, C.c_int32, _P, _P, C.c_uint32, C.c_int32, _P]),
+    "sarbp_upload_raw_blocks_bound_sm": (C.c_int, [_P, C.c_int64, _P, C.c_int64, _P, _P,
+                                                   C.c_int32, _P, _P, C.c_uint32, C.c_int32,
+                                                   _P]),
     "sarbp_stream_wait_flag": (C.c_int, [_P, _P, C.c_uint32]),
+    "sarbp_upload_host_arrays": (C.c_int, [C.c_int32, _P, _P, _P, _P]),
     "sarbp_focus_mixed_noalloc": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, _P, _P,
                                             _P, _P]),
     "sarbp_amplitude_u8": (C.c_int, [_P, C.c_int64, C.c_double, _P, _P, _P, C.c_size_t, _P]),

@@ -108,43 +108,69 @@ struct BlockEnds {
     int64_t end[kMaxBlocks];
 };
 
-__device__ __forceinline__ void copy_row16(float2 *__restrict__ drow, const float2 *__restrict__ srow,
-                                           int64_t lo, int64_t lo_up, int64_t hi, int64_t n2)
-{
-    if (threadIdx.x == 0) {
-        if (lo & 1) drow[lo] = srow[lo];
-        if ((hi & 1) && hi - 1 >= lo_up) drow[hi - 1] = srow[hi - 1];
-    }
-    const uint4 *s = reinterpret_cast<const uint4 *>(srow + lo_up);
-    uint4 *d = reinterpret_cast<uint4 *>(drow + lo_up);
-    for (int64_t i = threadIdx.x; i < n2; i += (int64_t)kCopyUnroll * kCopyThreads) {
-        uint4 v[kCopyUnroll];
-#pragma unroll
-        for (int u = 0; u < kCopyUnroll; ++u) {
-            const int64_t k = i + (int64_t)u * kCopyThreads;
-            if (k < n2) v[u] = s[k];
-        }
-#pragma unroll
-        for (int u = 0; u < kCopyUnroll; ++u) {
-            const int64_t k = i + (int64_t)u * kCopyThreads;
-            if (k < n2) d[k] = v[u];
-        }
-    }
-}
+// kBlockRows rows at a time, each thread holding kBlockSlots 16-byte words
+// of each: a CTA keeps up to 64 KB of loads from host memory in flight
+// (one row at a time kept ~13 KB, so it took ~64 SMs to fill the link).
+constexpr int kBlockRows = 4;
+constexpr int kBlockSlots = 4;
 
 __global__ void __launch_bounds__(kCopyThreads)
 gather_blocks16_kernel(float2 *__restrict__ dst, int64_t dpitch, const float2 *__restrict__ src,
-                       int64_t spitch, int64_t lo, int64_t n, const BlockEnds ends, int nblocks,
+                       int64_t spitch, int64_t lo, int64_t n, const int *__restrict__ bound,
+                       int64_t max_bins, const BlockEnds ends, int nblocks,
                        unsigned *__restrict__ counters, unsigned *__restrict__ flags,
                        unsigned generation)
 {
+    if (bound) {
+        // the inclusive bin interval [bound[0], bound[1]] (empty when
+        // bound[0] > bound[1]), clipped to the rows' first max_bins bins
+        __shared__ int64_t sb[2];
+        if (threadIdx.x == 0) {
+            const int64_t b0 = bound[0], b1 = bound[1];
+            const int64_t l = b0 < 0 ? 0 : b0, h = b1 > max_bins - 1 ? max_bins - 1 : b1;
+            sb[0] = l;
+            sb[1] = h >= l ? h - l + 1 : 0;
+        }
+        __syncthreads();
+        lo = sb[0];
+        n = sb[1];
+    }
     const int64_t lo_up = (lo + 1) & ~int64_t(1), hi = lo + n, hi_dn = hi & ~int64_t(1);
     const int64_t n2 = hi_dn > lo_up ? (hi_dn - lo_up) / 2 : 0;
+    constexpr int64_t kSpan = (int64_t)kBlockSlots * kCopyThreads;
     int64_t a0 = 0;
     for (int k = 0; k < nblocks; ++k) {
         const int64_t a1 = ends.end[k];
-        for (int64_t r = a0 + blockIdx.x; r < a1; r += gridDim.x)
-            copy_row16(dst + r * dpitch, src + r * spitch, lo, lo_up, hi, n2);
+        for (int64_t r0 = a0 + (int64_t)blockIdx.x * kBlockRows; r0 < a1;
+             r0 += (int64_t)gridDim.x * kBlockRows) {
+            if (n > 0 && threadIdx.x < kBlockRows && r0 + threadIdx.x < a1) {
+                // the odd bins at either end of the row, as single samples
+                const int64_t r = r0 + threadIdx.x;
+                if (lo & 1) dst[r * dpitch + lo] = src[r * spitch + lo];
+                if ((hi & 1) && hi - 1 >= lo_up) dst[r * dpitch + hi - 1] = src[r * spitch + hi - 1];
+            }
+            for (int64_t w0 = threadIdx.x; w0 < n2; w0 += kSpan) {
+                uint4 v[kBlockRows][kBlockSlots];
+#pragma unroll
+                for (int g = 0; g < kBlockRows; ++g) {
+                    const uint4 *s4 = reinterpret_cast<const uint4 *>(src + (r0 + g) * spitch + lo_up);
+#pragma unroll
+                    for (int u = 0; u < kBlockSlots; ++u) {
+                        const int64_t w = w0 + (int64_t)u * kCopyThreads;
+                        if (r0 + g < a1 && w < n2) v[g][u] = s4[w];
+                    }
+                }
+#pragma unroll
+                for (int g = 0; g < kBlockRows; ++g) {
+                    uint4 *d4 = reinterpret_cast<uint4 *>(dst + (r0 + g) * dpitch + lo_up);
+#pragma unroll
+                    for (int u = 0; u < kBlockSlots; ++u) {
+                        const int64_t w = w0 + (int64_t)u * kCopyThreads;
+                        if (r0 + g < a1 && w < n2) d4[w] = v[g][u];
+                    }
+                }
+            }
+        }
         __syncthreads();
         if (threadIdx.x == 0) {
             __threadfence();                      // this CTA's rows before its count
@@ -326,20 +352,40 @@ extern "C" SARBP_API int sarbp_copy_to_device_sm(void *dst, const void *src, int
     return cuda_status(cudaGetLastError(), "sarbp_copy_to_device_sm launch");
 }
 
-extern "C" SARBP_API int sarbp_upload_raw_blocks_sm(void *dst, int64_t dst_pitch, const void *src,
-                                                   int64_t src_pitch, int64_t bin_lo,
-                                                   int64_t nbins, const int64_t *block_ends,
-                                                   int32_t nblocks, uint32_t *flags,
-                                                   uint32_t *counters, uint32_t generation,
-                                                   int32_t ctas, void *stream)
+extern "C" SARBP_API int sarbp_upload_host_arrays(int32_t n, void *const *dst,
+                                                 const void *const *src, const int64_t *bytes,
+                                                 void *stream)
+{
+    if (n < 0 || (n > 0 && (!dst || !src || !bytes))) {
+        set_error("sarbp_upload_host_arrays: %d arrays, or a NULL list", n);
+        return SARBP_EINVAL;
+    }
+    for (int32_t i = 0; i < n; ++i)
+        if (bytes[i] < 0 || (bytes[i] > 0 && (!dst[i] || !src[i]))) {
+            set_error("sarbp_upload_host_arrays: array %d: NULL pointer or %lld bytes", i,
+                      (long long)bytes[i]);
+            return SARBP_EINVAL;
+        }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    for (int32_t i = 0; i < n; ++i) {
+        const int rc = h2d_bytes(dst[i], src[i], bytes[i], s);
+        if (rc) return rc;
+    }
+    return SARBP_OK;
+}
+
+static int upload_blocks(const char *who, void *dst, int64_t dst_pitch, const void *src,
+                         int64_t src_pitch, int64_t bin_lo, int64_t nbins, const int32_t *bound,
+                         const int64_t *block_ends, int32_t nblocks, uint32_t *flags,
+                         uint32_t *counters, uint32_t generation, int32_t ctas, void *stream)
 {
     if (!dst || !src || !block_ends || !flags || !counters || dst_pitch <= 0 || src_pitch <= 0 ||
-        bin_lo < 0 || nbins <= 0 || bin_lo + nbins > dst_pitch || bin_lo + nbins > src_pitch ||
+        bin_lo < 0 || nbins < 0 || bin_lo + nbins > dst_pitch || bin_lo + nbins > src_pitch ||
         nblocks <= 0 || nblocks > kMaxBlocks || ctas <= 0 || generation == 0 ||
         (dst_pitch & 1) || (src_pitch & 1) || (reinterpret_cast<uintptr_t>(dst) & 15)) {
-        set_error("sarbp_upload_raw_blocks_sm: bad pointers, bin range [%lld, +%lld), pitches "
-                  "%lld / %lld (both even), %d blocks (1..%d), %d CTAs or generation 0",
-                  (long long)bin_lo, (long long)nbins, (long long)dst_pitch,
+        set_error("%s: bad pointers, bin range [%lld, +%lld), pitches %lld / %lld (both even), "
+                  "%d blocks (1..%d), %d CTAs or generation 0",
+                  who, (long long)bin_lo, (long long)nbins, (long long)dst_pitch,
                   (long long)src_pitch, nblocks, kMaxBlocks, ctas);
         return SARBP_EINVAL;
     }
@@ -347,25 +393,63 @@ extern "C" SARBP_API int sarbp_upload_raw_blocks_sm(void *dst, int64_t dst_pitch
     int64_t prev = 0;
     for (int k = 0; k < nblocks; ++k) {
         if (block_ends[k] < prev) {
-            set_error("sarbp_upload_raw_blocks_sm: block ends must not decrease");
+            set_error("%s: block ends must not decrease", who);
             return SARBP_EINVAL;
         }
         e.end[k] = prev = block_ends[k];
     }
     const void *sv = device_view(src);
     if (!sv || (reinterpret_cast<uintptr_t>(sv) & 15)) {
-        set_error("sarbp_upload_raw_blocks_sm: the source is not 16-byte aligned page-locked "
-                  "host memory mapped into the device's address space (or device memory)");
+        set_error("%s: the source is not 16-byte aligned page-locked host memory mapped into "
+                  "the device's address space (or device memory)", who);
         return SARBP_EINVAL;
     }
+    const int *bv = nullptr;
+    if (bound) {
+        bv = static_cast<const int *>(device_view(bound));
+        if (!bv) {
+            set_error("%s: the bound is neither device memory nor page-locked host memory", who);
+            return SARBP_EINVAL;
+        }
+    }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    int rc = cuda_status(cudaMemsetAsync(counters, 0, sizeof(uint32_t) * nblocks, s),
-                         "sarbp_upload_raw_blocks_sm: counters");
+    int rc = cuda_status(cudaMemsetAsync(counters, 0, sizeof(uint32_t) * nblocks, s), who);
     if (rc) return rc;
+    const int64_t max_bins = dst_pitch < src_pitch ? dst_pitch : src_pitch;
     gather_blocks16_kernel<<<ctas, kCopyThreads, 0, s>>>(
         static_cast<float2 *>(dst), dst_pitch, static_cast<const float2 *>(sv), src_pitch, bin_lo,
-        nbins, e, nblocks, counters, flags, generation);
-    return cuda_status(cudaGetLastError(), "sarbp_upload_raw_blocks_sm launch");
+        nbins, bv, max_bins, e, nblocks, counters, flags, generation);
+    return cuda_status(cudaGetLastError(), who);
+}
+
+extern "C" SARBP_API int sarbp_upload_raw_blocks_sm(void *dst, int64_t dst_pitch, const void *src,
+                                                   int64_t src_pitch, int64_t bin_lo,
+                                                   int64_t nbins, const int64_t *block_ends,
+                                                   int32_t nblocks, uint32_t *flags,
+                                                   uint32_t *counters, uint32_t generation,
+                                                   int32_t ctas, void *stream)
+{
+    if (nbins <= 0) {
+        set_error("sarbp_upload_raw_blocks_sm: no bins (%lld)", (long long)nbins);
+        return SARBP_EINVAL;
+    }
+    return upload_blocks("sarbp_upload_raw_blocks_sm", dst, dst_pitch, src, src_pitch, bin_lo,
+                         nbins, nullptr, block_ends, nblocks, flags, counters, generation, ctas,
+                         stream);
+}
+
+extern "C" SARBP_API int sarbp_upload_raw_blocks_bound_sm(
+    void *dst, int64_t dst_pitch, const void *src, int64_t src_pitch, const int32_t *bound,
+    const int64_t *block_ends, int32_t nblocks, uint32_t *flags, uint32_t *counters,
+    uint32_t generation, int32_t ctas, void *stream)
+{
+    if (!bound) {
+        set_error("sarbp_upload_raw_blocks_bound_sm: bound is NULL");
+        return SARBP_EINVAL;
+    }
+    return upload_blocks("sarbp_upload_raw_blocks_bound_sm", dst, dst_pitch, src, src_pitch, 0,
+                         0, bound, block_ends, nblocks, flags, counters, generation, ctas,
+                         stream);
 }
 
 namespace {

@@ -22,7 +22,8 @@ import numpy as np
 import torch
 
 from . import _lib
-from .scene import DeviceScene, _pulse_major_host, scene_to_device
+from .scene import (DeviceScene, _bound_reached_bins_async, _pulse_major_host,
+                    read_bound, scene_to_device)
 
 PRECISIONS = ("fp64", "mixed")
 
@@ -138,7 +139,9 @@ def FocalizzatoreBpPx(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
         img, scene = _focus_streamed((xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz,
                                       Raw_Data, near_range, dra, lambda_val, Sint), t, device)
         last_call.update(h2d_bytes=scene.h2d_bytes, d2h_bytes=img.nbytes,
-                         raw_bins=(scene.bin_lo, scene.bin_hi), streamed=True)
+                         raw_bins=(scene.bin_lo, scene.bin_hi), streamed=True,
+                         upload=scene.upload,
+                         small_upload=getattr(scene, "small_upload", "per-array"))
         return img
     scene = scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
                             near_range, dra, lambda_val, Sint, device=device, raw_bins="reached")
@@ -151,19 +154,28 @@ def FocalizzatoreBpPx(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
 
 
 STREAM_BLOCKS = 8      # pulse blocks of a streamed drop-in upload
-# how the streamed drop-in copies the reachable raw bins from page-locked
-# host memory: "sm" (SM loads of 16-byte words, one CTA per SM, on a stream of
-# the highest priority, so its CTAs take SMs as focusing CTAs finish) or
-# "copy" (copy engine).  Measured over 240 calls each on the full workload:
-# SM loads 3.89 ms mean, 3.85 ms median, 4.09 ms at the 99th percentile; the
-# copy engine 4.17 ms mean, 3.41 ms median, 9.5 ms at the 99th percentile and
-# 86 ms worst (its host-to-device stalls).  "signal": one persistent copy
-# kernel of SIGNAL_CTAS CTAs that sets a device flag per finished block, each
-# focusing segment's stream held behind its flag; over 200 calls 3.89 ms mean
-# at 64 CTAs (16: 5.97, 32: 4.23, 96: 4.28, 152: 5.03 ms; fewer CTAs cannot
-# keep the host link busy, more take SMs from focusing), a tie with "sm"
-STREAM_UPLOAD = "sm"
-SIGNAL_CTAS = 64       # "signal": CTAs of the persistent block-copy kernel
+# the final block is halved STREAM_TAIL times: the tiles whose apertures end
+# in the last pulses (all those clipped at the scene's end) wait for the
+# final rows, so the last blocks are kept short
+STREAM_TAIL = 3
+STREAM_LANES = 3       # compute streams the focusing segments rotate over
+# "one-call": the DEM, masks and trajectory go up in one foreign call when
+# their dtypes and layout need no conversion; "torch": per-array copies
+SMALL_UPLOAD = "one-call"
+# How the streamed drop-in copies the reachable raw bins from page-locked
+# host memory.  "signal" (default): the host does not wait for the bin bound;
+# one persistent copy kernel of SIGNAL_CTAS CTAs (four rows, 64 KB of loads
+# in flight per CTA) reads the bound, copies the blocks in order and sets a
+# device flag per finished block, and each focusing segment's stream is held
+# behind its block's flag.  "sm": per-block SM-load copies (one CTA per SM,
+# highest-priority stream) after a host wait for the bound.  "copy": the
+# copy engine per block.  Pageable raw rows always take the copy engine.
+# Full workload, 200 calls each, one run: "signal" 3.52 ms mean, 3.54 ms at
+# the 99th percentile (24 CTAs 3.69, 32: 3.55, 48: 3.57); "sm" 3.99 / 4.31;
+# the copy engine's median is 3.41 ms but it stalls for tens of ms now and
+# then (p99 9.5 ms, worst 86 ms in an earlier run).
+STREAM_UPLOAD = "signal"
+SIGNAL_CTAS = 40       # "signal": CTAs of the persistent block-copy kernel
 FRESH_AHEAD = 2        # result arrays the drop-in call keeps faulted in ahead
 
 
@@ -243,9 +255,30 @@ class _DropIn:
         self.counters = torch.zeros(32, dtype=torch.int32, device=dev)
         self.generation = 0
         self.side = torch.cuda.Stream(dev)
+        self.side2 = torch.cuda.Stream(dev)
+        self.bound_host = torch.zeros(2, dtype=torch.int32).pin_memory()
         self.raw: dict[tuple, torch.Tensor] = {}
         self.out: dict[int, torch.Tensor] = {}
+        self.small: dict[tuple, tuple] = {}
         self.images = FreshImages()
+
+    def small_buffers(self, npix: int, naz: int, dev) -> tuple:
+        """One device buffer for the DEM, masks and trajectory of a scene
+        shape: (views by DeviceScene field name, device addresses, bytes)."""
+        key = (npix, naz)
+        if key not in self.small:
+            self.small.clear()
+            sizes = [npix * 8] * 3 + [npix, npix * 4, npix * 4] + [naz * 8] * 3
+            offs, o = [], 0
+            for b in sizes:
+                offs.append(o)
+                o += -(-b // 256) * 256
+            buf = torch.empty(max(o, 1), dtype=torch.uint8, device=dev)
+            views = {name: buf[off:off + b].view(dt)
+                     for (name, dt), off, b in zip(_SMALL_FIELDS, offs, sizes)}
+            dptrs = (C.c_void_p * 9)(*[views[n].data_ptr() for n, _ in _SMALL_FIELDS])
+            self.small[key] = (views, dptrs, (C.c_int64 * 9)(*sizes), sum(sizes))
+        return self.small[key]
 
     def raw_buffer(self, nra: int, naz: int, dev) -> torch.Tensor:
         key = (naz, nra + (nra & 1))
@@ -270,6 +303,7 @@ def release_drop_in_buffers() -> None:
         with r.lock:
             r.raw.clear()
             r.out.clear()
+            r.small.clear()
             r.images.clear()
 
 
@@ -285,9 +319,13 @@ def _focus_streamed(args, t: _lib.Tuning, device, blocks: int = STREAM_BLOCKS):
 
     The queue of the scene's tiles is ordered by last aperture pulse
     (staged=3); the reachable range bins of the pulse rows go up in
-    ``blocks`` pulse blocks on a copy stream, and after each block the
-    queue items whose pulses are all resident are focused on the compute
-    stream.  Returns (image, scene).
+    ``blocks`` pulse blocks (the last one halved STREAM_TAIL times) on a copy
+    stream, and after each block the queue items whose pulses are all
+    resident are focused, the segments rotating over STREAM_LANES streams.
+    With STREAM_UPLOAD "signal" and page-locked raw rows the small inputs go
+    up in one call, the host never waits for the bin bound, and the blocks
+    come from one persistent copy kernel whose per-block device flags the
+    segments' streams wait on.  Returns (image, scene).
     """
     lib = _lib.load()
     tq = _lib.Tuning.from_buffer_copy(t)
@@ -299,79 +337,155 @@ def _focus_streamed(args, t: _lib.Tuning, device, blocks: int = STREAM_BLOCKS):
         return _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache)
 
 
+# DeviceScene fields held in the drop-in's small-array buffer, in order
+_SMALL_FIELDS = (("x", torch.float64), ("y", torch.float64), ("z", torch.float64),
+                 ("mask", torch.uint8), ("index", torch.int32), ("sint", torch.int32),
+                 ("tx", torch.float64), ("ty", torch.float64), ("tz", torch.float64))
+_NP_OF = {torch.float64: np.dtype(np.float64), torch.uint8: np.dtype(np.uint8),
+          torch.int32: np.dtype(np.int32)}
+
+
+def _column_major_words(a, dt: torch.dtype, n: int, exact: bool):
+    """Host address of an array of dtype ``dt`` whose column-major flatten
+    (the reference's ``flatten(order='F')``) is its memory order, with n
+    elements (at least n unless ``exact``); None otherwise."""
+    if isinstance(a, np.ndarray):
+        if (a.dtype != _NP_OF[dt] or not a.flags.f_contiguous
+                or (a.size != n if exact else a.size < n)):
+            return None
+        return a.__array_interface__["data"][0]
+    if isinstance(a, torch.Tensor):
+        if (a.device.type != "cpu" or a.dtype != dt
+                or (a.numel() != n if exact else a.numel() < n)):
+            return None
+        expect = 1
+        for size, stride in zip(a.shape, a.stride()):
+            if size != 1 and stride != expect:
+                return None
+            expect *= size
+        return a.data_ptr()
+    return None
+
+
+def _scene_from_host(args, dev, lib, res_cache: _DropIn, raw_buffer, host_rows):
+    """The drop-in's DeviceScene without per-array Python work: when every
+    DEM, mask and trajectory argument already has the dtype the reference
+    casts it to and column-major memory order, all nine go up in one
+    sarbp_upload_host_arrays call into the per-shape buffer.  None when an
+    argument needs a cast, a copy or a check (scene_to_device does those)."""
+    (xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, raw, near_range, dra, lambda_val,
+     sint) = args
+    if len(tuple(xxg1.shape)) != 2:
+        return None
+    dim0, dim1 = (int(v) for v in xxg1.shape)
+    npix = dim0 * dim1
+    nra, naz = (int(v) for v in raw.shape)
+    srcs = []
+    for a, (_, dt) in zip((xxg1, yyg1, zzg1, mask, index, sint), _SMALL_FIELDS):
+        srcs.append(_column_major_words(a, dt, npix, True))
+    for w in (wgsx, wgsy, wgsz):
+        srcs.append(_column_major_words(w, torch.float64, naz, False))
+    if any(p is None for p in srcs):
+        return None
+    views, dptrs, sizes, total = res_cache.small_buffers(npix, naz, dev)
+    _lib.check(lib.sarbp_upload_host_arrays(9, dptrs, (C.c_void_p * 9)(*srcs), sizes,
+                                            torch.cuda.current_stream(dev).cuda_stream))
+    scene = DeviceScene(dim0=dim0, dim1=dim1, raw=raw_buffer, nra=nra, naz=naz,
+                        pitch=nra + (nra & 1), near_range=float(near_range),
+                        delta_range=float(dra), lambda_=float(lambda_val),
+                        **{name: views[name] for name, _ in _SMALL_FIELDS})
+    scene.h2d_bytes = total
+    scene.host_rows = host_rows
+    scene.small_upload = "one-call"
+    return scene
+
+
+def _stream_marks(naz: int, blocks: int, tail: int) -> list[int]:
+    """Pulse block ends: ``blocks`` equal blocks, the last one halved
+    ``tail`` times (at most 32 ends)."""
+    marks = [naz * (k + 1) // blocks for k in range(blocks - 1)]
+    for h in range(1, tail + 1):
+        marks.append(naz - naz // (blocks << h))
+    marks.append(naz)
+    return marks[-32:] if len(marks) > 32 else marks
+
+
 def _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache: _DropIn):
     nra, naz = (int(v) for v in tuple(args[8].shape))
-    scene = scene_to_device(*args, device=dev, raw_bins="bound", tuning=tq,
-                            raw_buffer=res_cache.raw_buffer(nra, naz, dev))
+    host_rows = _pulse_major_host(args[8])
+    # "signal": the bound is not waited for; the persistent block copy reads
+    # it from page-locked memory once the stream has computed it
+    signal = (STREAM_UPLOAD == "signal" and host_rows is not None and host_rows.is_pinned()
+              and nra % 2 == 0 and host_rows.data_ptr() % 16 == 0)
+    raw_buffer = res_cache.raw_buffer(nra, naz, dev)
+    if not signal:
+        scene = scene_to_device(*args, device=dev, raw_bins="bound", tuning=tq,
+                                raw_buffer=raw_buffer)
+    else:
+        scene = None
+        if SMALL_UPLOAD == "one-call":
+            scene = _scene_from_host(args, dev, lib, res_cache, raw_buffer, host_rows)
+        if scene is None:
+            scene = scene_to_device(*args, device=dev, raw_bins="deferred", tuning=tq,
+                                    raw_buffer=raw_buffer, bound_host=res_cache.bound_host)
+        else:
+            _bound_reached_bins_async(scene, res_cache.bound_host, tuning=tq)
     compute = torch.cuda.current_stream(dev)
     sc = C.byref(scene.struct())
     ws = scene.workspace
+    marks = _stream_marks(scene.naz, blocks, STREAM_TAIL)
+    side, side2 = res_cache.side, res_cache.side2
+    lanes = (compute, side, side2)[:max(1, min(3, STREAM_LANES))]
+    for lane in lanes[1:]:
+        lane.wait_stream(compute)
+        ws.record_stream(lane)
+    out = res_cache.out_buffer(scene.npix, dev)
+    if signal:
+        copy = res_cache.copy_sm
+        copy.wait_stream(compute)           # bound, raw buffer and tables on compute
+        res_cache.generation = res_cache.generation % 0xFFFFFFFF + 1
+        gen = res_cache.generation
+        block_ends = np.asarray(marks, dtype=np.int64)
+        _lib.check(lib.sarbp_upload_raw_blocks_bound_sm(
+            scene.raw.data_ptr(), scene.pitch, host_rows.data_ptr(), nra,
+            res_cache.bound_host.data_ptr(), block_ends.ctypes.data, len(marks),
+            res_cache.flags.data_ptr(), res_cache.counters.data_ptr(), gen, SIGNAL_CTAS,
+            copy.cuda_stream))
     nt = _lib.check(int(lib.sarbp_tile_count(sc, C.byref(tq))))
     keys = np.empty(nt, dtype=np.uint32)
     _lib.check(lib.sarbp_tile_queue_keys(sc, C.byref(tq), ws.data_ptr(), ws.numel(),
                                          keys.ctypes.data_as(C.POINTER(C.c_uint32)), nt,
                                          compute.cuda_stream))
-    out = res_cache.out_buffer(scene.npix, dev)
-    lo, hi = scene.bin_lo, scene.bin_hi
-    naz = scene.naz
-    # equal pulse blocks, the last one split in two: the tiles that end in
-    # the final block are the only work left after the copies, so it is small
-    marks = [naz * (k + 1) // blocks for k in range(blocks - 1)]
-    marks += [naz - naz // (2 * blocks), naz]
     ends = np.searchsorted(keys, np.asarray(marks, dtype=np.int64), side="right")
     ends[-1] = nt
-    pinned = scene.host_rows.is_pinned()
-    sm = STREAM_UPLOAD in ("sm", "signal") and pinned
-    signal = (STREAM_UPLOAD == "signal" and pinned and hi >= lo and len(marks) <= 32
-              and scene.nra % 2 == 0 and scene.pitch % 2 == 0
-              and scene.host_rows.data_ptr() % 16 == 0 and scene.raw.data_ptr() % 16 == 0)
-    copy = res_cache.copy_sm if sm else res_cache.copy
-    upload = lib.sarbp_upload_raw_bins_sm if sm else lib.sarbp_upload_raw_bins
-    copy.wait_stream(compute)               # raw buffer and tables allocated on compute
-    # segments alternate between two compute streams so that one segment's
-    # last CTAs overlap the next segment's first
-    side = res_cache.side
-    side.wait_stream(compute)
-    ws.record_stream(side)
-    lanes = (compute, side)
+    if signal:
+        lo, hi = read_bound(scene)           # the keys' synchronisation passed the bound
+    else:
+        lo, hi = scene.bin_lo, scene.bin_hi
+        sm = STREAM_UPLOAD in ("sm", "signal") and scene.host_rows.is_pinned()
+        copy = res_cache.copy_sm if sm else res_cache.copy
+        upload = lib.sarbp_upload_raw_bins_sm if sm else lib.sarbp_upload_raw_bins
+        copy.wait_stream(compute)           # raw buffer and tables allocated on compute
     row = scene.pitch * 8
     first = 0
     a0 = 0
-    if signal:
-        # one persistent copy kernel on SIGNAL_CTAS SMs; each segment's stream
-        # waits for its block's flag, so focusing runs beside the copy
-        res_cache.generation = res_cache.generation % 0xFFFFFFFF + 1
-        gen = res_cache.generation
-        block_ends = np.asarray(marks, dtype=np.int64)
-        _lib.check(lib.sarbp_upload_raw_blocks_sm(
-            scene.raw.data_ptr(), scene.pitch, scene.host_rows.data_ptr(), scene.nra, lo,
-            hi - lo + 1, block_ends.ctypes.data, len(marks), res_cache.flags.data_ptr(),
-            res_cache.counters.data_ptr(), gen, SIGNAL_CTAS, copy.cuda_stream))
-        scene.h2d_bytes += (hi - lo + 1) * naz * 8
-        for k in range(len(marks)):
-            lane = lanes[k % 2]
-            _lib.check(lib.sarbp_stream_wait_flag(lane.cuda_stream,
-                                                  res_cache.flags.data_ptr() + 4 * k, gen))
-            count = int(ends[k]) - first
-            if count > 0:
-                _lib.check(lib.sarbp_focus_mixed_range(sc, C.byref(tq), out.data_ptr(), None,
-                                                       None, None, ws.data_ptr(), ws.numel(),
-                                                       first, count, lane.cuda_stream))
-            first = int(ends[k])
-        marks = []                                  # nothing left for the loop below
-        compute.wait_stream(copy)
     for k in range(len(marks)):
         a1 = marks[k]
-        if hi >= lo and a1 > a0:
-            _lib.check(upload(
-                scene.raw.data_ptr() + a0 * row, scene.pitch,
-                scene.host_rows.data_ptr() + a0 * scene.nra * 8, scene.nra, lo, hi - lo + 1,
-                a1 - a0, copy.cuda_stream))
-            scene.h2d_bytes += (hi - lo + 1) * (a1 - a0) * 8
-        ev = torch.cuda.Event()
-        ev.record(copy)
-        lane = lanes[k % 2]
-        lane.wait_event(ev)
+        lane = lanes[k % len(lanes)]
+        if signal:
+            # each segment's stream waits for its block's flag, so focusing
+            # runs beside the copy kernel
+            _lib.check(lib.sarbp_stream_wait_flag(lane.cuda_stream,
+                                                  res_cache.flags.data_ptr() + 4 * k, gen))
+        else:
+            if hi >= lo and a1 > a0:
+                _lib.check(upload(
+                    scene.raw.data_ptr() + a0 * row, scene.pitch,
+                    scene.host_rows.data_ptr() + a0 * scene.nra * 8, scene.nra, lo,
+                    hi - lo + 1, a1 - a0, copy.cuda_stream))
+            ev = torch.cuda.Event()
+            ev.record(copy)
+            lane.wait_event(ev)
         count = int(ends[k]) - first
         if count > 0:
             _lib.check(lib.sarbp_focus_mixed_range(sc, C.byref(tq), out.data_ptr(), None, None,
@@ -379,7 +493,12 @@ def _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache: _DropIn):
                                                    count, lane.cuda_stream))
         first = int(ends[k])
         a0 = a1
-    compute.wait_stream(side)
+    if hi >= lo:
+        scene.h2d_bytes += (hi - lo + 1) * naz * 8
+    scene.upload = "signal" if signal else ("sm" if sm else "copy")
+    for lane in lanes[1:]:
+        compute.wait_stream(lane)
+    compute.wait_stream(copy)
     res = FocusResult(image=out, workspace=ws)
     img = res_cache.images.get(scene.dim0, scene.dim1)
     # column-major pixels: the F-order array's memory is the device image's

@@ -152,7 +152,22 @@ def test_new_entry_points_reject_bad_arguments_without_a_gpu():
     a[6], a[7] = desc, 3
     assert lib.sarbp_upload_raw_blocks_sm(*a) == _lib.SARBP_EINVAL
     assert "decrease" in _lib.last_error()
+    assert lib.sarbp_upload_raw_blocks_bound_sm(C.c_void_p(0x1000), 100, C.c_void_p(0x2000),
+                                                100, None, ends, 4, fl, ct, 1, 8,
+                                                None) == _lib.SARBP_EINVAL
+    assert lib.sarbp_upload_raw_blocks_bound_sm(C.c_void_p(0x1000), 101, C.c_void_p(0x2000),
+                                                100, C.c_void_p(0x7000), ends, 4, fl, ct, 1, 8,
+                                                None) == _lib.SARBP_EINVAL
     assert lib.sarbp_stream_wait_flag(None, None, 1) == _lib.SARBP_EINVAL
+    # one-call uploads: a negative count, a NULL list or a NULL array with bytes
+    assert lib.sarbp_upload_host_arrays(-1, None, None, None, None) == _lib.SARBP_EINVAL
+    assert lib.sarbp_upload_host_arrays(2, None, None, None, None) == _lib.SARBP_EINVAL
+    dsts = (C.c_void_p * 2)(0x1000, None)
+    srcs = (C.c_void_p * 2)(0x2000, 0x3000)
+    nbytes = (C.c_int64 * 2)(0, 16)
+    assert lib.sarbp_upload_host_arrays(2, dsts, srcs, nbytes, None) == _lib.SARBP_EINVAL
+    assert "array 1" in _lib.last_error()
+    assert lib.sarbp_upload_host_arrays(0, None, None, None, None) == _lib.SARBP_OK
     s = _lib.Scene()
     s.dim0, s.dim1 = 64, 16
     for f in ("dem_x", "dem_y", "dem_z", "mask", "index", "sint", "traj_x", "traj_y",

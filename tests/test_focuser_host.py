@@ -130,3 +130,39 @@ def test_serving_engine_checks_its_options_before_the_device():
         serve.ServingEngine(device="cpu", h2d="dma")
     with pytest.raises(ValueError, match="policy"):
         serve.ServingEngine(device="cpu", policy="lifo")
+
+
+@pytest.mark.parametrize("naz,blocks,tail", [(40001, 8, 1), (40001, 8, 3), (2001, 4, 0),
+                                             (37, 8, 2), (40001, 30, 4)])
+def test_stream_marks_cover_the_pulses_with_a_short_tail(naz, blocks, tail):
+    from sar_backprojection_gb300.focuser import _stream_marks
+
+    m = _stream_marks(naz, blocks, tail)
+    assert m[-1] == naz and len(m) <= 32
+    assert all(a <= b for a, b in zip(m, m[1:]))
+    if len(m) == blocks + tail:
+        # the final blocks halve
+        lens = np.diff([0] + m)
+        assert all(lens[-1 - h] <= (naz // blocks) // (1 << h) + 1 for h in range(tail))
+
+
+def test_one_call_upload_takes_only_arrays_that_need_no_conversion():
+    """The drop-in's one-call upload accepts column-major arrays of the
+    reference's dtypes (NumPy F-order, a transposed C-contiguous tensor) and
+    leaves everything else to the per-array path."""
+    from sar_backprojection_gb300.focuser import _column_major_words
+
+    f = np.asfortranarray(np.zeros((6, 4)))
+    assert _column_major_words(f, torch.float64, 24, True) == f.__array_interface__["data"][0]
+    assert _column_major_words(np.zeros((6, 4)), torch.float64, 24, True) is None   # C order
+    assert _column_major_words(f.astype(np.float32), torch.float64, 24, True) is None
+    assert _column_major_words(f, torch.float64, 23, True) is None                  # size
+    assert _column_major_words(f[:, :3], torch.float64, 18, True) is not None        # F slice
+    assert _column_major_words(f[::2], torch.float64, 12, True) is None              # strided
+    t = torch.zeros((4, 6), dtype=torch.int32).t()
+    assert _column_major_words(t, torch.int32, 24, True) == t.data_ptr()
+    assert _column_major_words(t.t(), torch.int32, 24, True) is None
+    w = np.zeros(11)
+    assert _column_major_words(w, torch.float64, 10, False) is not None               # >= naz
+    assert _column_major_words(w, torch.float64, 12, False) is None
+    assert _column_major_words([1.0, 2.0], torch.float64, 2, False) is None

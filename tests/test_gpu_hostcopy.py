@@ -97,6 +97,33 @@ def test_signalled_blocks_match_the_copy_engine(lib, naz, nra, dpitch, lo, nb, e
         assert counters[:len(ends)].tolist() == [ctas] * len(ends)
 
 
+@pytest.mark.parametrize("where", ["pinned", "device"])
+@pytest.mark.parametrize("bound", [(123, 639), (0, 5000), (-7, 3), (1, 0), (900, 100)])
+def test_blocks_read_their_bound_from_memory(lib, where, bound):
+    """The bound-reading block copy equals the copy engine over the bound
+    clipped to the rows; an empty bound copies nothing and still sets every
+    flag."""
+    naz, nra = 97, 1000
+    host = torch.randn((naz, nra, 2), dtype=torch.float32).pin_memory()
+    b = torch.tensor(bound, dtype=torch.int32)
+    b = b.pin_memory() if where == "pinned" else b.cuda()
+    lo, hi = max(bound[0], 0), min(bound[1], nra - 1)
+    a = torch.full((naz, nra, 2), 7.0, device="cuda")
+    got = a.clone()
+    if hi >= lo:
+        _lib.check(lib.sarbp_upload_raw_bins(a.data_ptr(), nra, host.data_ptr(), nra, lo,
+                                             hi - lo + 1, naz, _stream()))
+    flags = torch.zeros(32, dtype=torch.int32, device="cuda")
+    counters = torch.zeros(32, dtype=torch.int32, device="cuda")
+    ends = np.asarray([10, 50, 97], dtype=np.int64)
+    _lib.check(lib.sarbp_upload_raw_blocks_bound_sm(
+        got.data_ptr(), nra, host.data_ptr(), nra, b.data_ptr(), ends.ctypes.data, 3,
+        flags.data_ptr(), counters.data_ptr(), 5, 16, _stream()))
+    torch.cuda.synchronize()
+    assert torch.equal(got, a)
+    assert flags[:3].tolist() == [5, 5, 5]
+
+
 def test_pageable_source_is_rejected(lib):
     src = np.zeros(4096, dtype=np.uint8)                 # not page-locked
     dst = torch.zeros(4096, dtype=torch.uint8, device="cuda")

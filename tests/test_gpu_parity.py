@@ -234,26 +234,37 @@ def test_full_workload_production_launch(full_scene, full_oracle, tuning):
                                                           "rms_phase_mrad")})
 
 
-@pytest.mark.parametrize("upload", ["sm", "signal", "copy"])
-def test_full_workload_streamed_drop_in(full_scene, full_oracle, upload, monkeypatch):
+@pytest.mark.parametrize("upload,pinned", [("signal", True), ("sm", True), ("copy", True),
+                                           ("signal", False)])
+def test_full_workload_streamed_drop_in(full_scene, full_oracle, upload, pinned, monkeypatch):
     """The drop-in call as the bench's e2e measures it: host inputs in the
     reference's layout, precision="mixed" with the bench's preferred tuning,
     the reachable range bins streamed up in pulse blocks while focusing runs
     (by each upload mode: SM loads per block, one persistent block copy that
-    signals each block through a device flag, the copy engine).  The
-    returned image must equal the resident launch of the same tuning bit for
-    bit (whose range bins equal the oracle's) and meet the bars against the
-    oracle."""
+    signals each block through a device flag, the copy engine; page-locked
+    raw rows, and pageable ones, which take the copy engine in every mode).
+    The returned image must equal the resident launch of the same tuning bit
+    for bit (whose range bins equal the oracle's) and meet the bars against
+    the oracle."""
     from sar_backprojection_gb300 import FocalizzatoreBpPx, focuser
 
     monkeypatch.setattr(focuser, "STREAM_UPLOAD", upload)
     oimg, onv, ocs = full_oracle
     tuning = _bench_tunings()[0]
     host = dict(full_scene)
-    host["RawData"] = full_scene["RawData"].cpu()       # (nra, naz), pulse-major memory
+    raw = full_scene["RawData"]                          # (nra, naz), pulse-major memory
+    if pinned:
+        rows = torch.empty((raw.shape[1], raw.shape[0]), dtype=raw.dtype, pin_memory=True)
+        rows.copy_(raw.t())
+        host["RawData"] = rows.t()
+    else:
+        host["RawData"] = raw.cpu()
     for _ in range(2):                                   # second call: next flag generation
         img = FocalizzatoreBpPx(*synth.focus_args(host), precision="mixed", tuning=tuning)
     assert focuser.last_call["streamed"]
+    assert focuser.last_call["upload"] == (upload if pinned else "copy")
+    if upload == "signal" and pinned:
+        assert focuser.last_call["small_upload"] == "one-call"
     assert img.shape == (4000, 250) and img.dtype == np.complex128
     ds = scene_to_device(*synth.focus_args(full_scene))
     diag = focus(ds, "mixed", tuning=tuning, diagnostics=True).check()
