@@ -811,6 +811,9 @@ def run_ours(args, dist: Dist):
                "value_at_p50": dist.world * work / float(np.percentile(times, 50)) / 1e9,
                "calls_ms": [round(1e3 * x, 3) for x in times],
                "streamed": bool(_focuser.last_call.get("streamed")),
+               "upload": _focuser.last_call.get("upload"),
+               "small_upload": _focuser.last_call.get("small_upload"),
+               "d2h": _focuser.last_call.get("d2h"),
                "what": "pinned host inputs; the call copies the DEM, masks, trajectory and the "
                        "range bins the apertures can reach (device-computed bound) in pulse "
                        "blocks overlapped by focusing, and returns the complex128 image in "
@@ -852,10 +855,14 @@ def run_ours(args, dist: Dist):
                 "max_ms": 1e3 * max(ptimes),
                 "h2d_bytes_per_step": int(_focuser.last_call["h2d_bytes"]),
                 "d2h_bytes_per_step": int(d2h),
+                "upload": _focuser.last_call.get("upload"),
+                "d2h": _focuser.last_call.get("d2h"),
+                "device_reads_pageable": bool(_lib.load().sarbp_device_reads_pageable()),
                 "what": "plain NumPy arrays in pageable host memory, as the reference's "
-                        "script passes them; the driver stages pageable copies through "
-                        "its own pinned buffers, so each pulse block's upload holds the "
-                        "host thread"}
+                        "script passes them; on a device that reaches pageable memory "
+                        "through the host's page tables the call's copy kernels read "
+                        "them (and write the result array) in place, elsewhere the "
+                        "driver stages them through its own pinned buffers"}
             del raw_np, np_args
         ts = sorted(times)
         lat = {"p50_ms": 1e3 * float(np.percentile(ts, 50)),

@@ -276,6 +276,25 @@ SARBP_API int sarbp_upload_host_arrays(int32_t n, void *const *dst, const void *
                                        const int64_t *bytes, void *stream);
 
 /*
+ * 1 when the current device loads from and stores to pageable host memory
+ * through the host's page tables (cudaDevAttrPageableMemoryAccess and
+ * ...UsesHostPageTables: coherent CPU-GPU systems such as GB300 over
+ * NVLink-C2C), else 0.  On such a device every SM-load copy above also takes
+ * plain (pageable) host memory, read in place at the link's rate rather than
+ * staged by the driver.  No reference counterpart.
+ */
+SARBP_API int sarbp_device_reads_pageable(void);
+
+/*
+ * Device-to-host copy by SM stores: `bytes` bytes from device memory `src`
+ * into page-locked host memory (through its mapping) or, on a device that
+ * reads pageable memory (above), into any host memory.  Stream-ordered; the
+ * data are in host memory once the stream has passed the copy.  The drop-in
+ * call writes its fresh result array this way.  No reference counterpart.
+ */
+SARBP_API int sarbp_copy_to_host_sm(void *dst, const void *src, int64_t bytes, void *stream);
+
+/*
  * The same rows in pulse blocks, copied by one persistent grid of `ctas`
  * CTAs that signals each block: block k is rows [block_ends[k-1],
  * block_ends[k]) (block_ends non-decreasing, at most 32 blocks); when every

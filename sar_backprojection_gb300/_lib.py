@@ -111,6 +111,8 @@ SIGNATURES = {
                                                    _P]),
     "sarbp_stream_wait_flag": (C.c_int, [_P, _P, C.c_uint32]),
     "sarbp_upload_host_arrays": (C.c_int, [C.c_int32, _P, _P, _P, _P]),
+    "sarbp_device_reads_pageable": (C.c_int, []),
+    "sarbp_copy_to_host_sm": (C.c_int, [_P, _P, C.c_int64, _P]),
     "sarbp_focus_mixed_noalloc": (C.c_int, [C.POINTER(Scene), C.POINTER(Tuning), _P, _P, _P,
                                             _P, _P]),
     "sarbp_amplitude_u8": (C.c_int, [_P, C.c_int64, C.c_double, _P, _P, _P, C.c_size_t, _P]),

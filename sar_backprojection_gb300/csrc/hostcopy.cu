@@ -9,26 +9,55 @@
 // A caller that mostly waits on uploads rather than on kernels (the serving
 // loop) gets a steadier latency from these copies.  The source must be
 // page-locked host memory mapped into the device's address space (what
-// cudaHostAlloc / torch pin_memory give) or device memory; anything else is
-// rejected before any launch.
+// cudaHostAlloc / torch pin_memory give), device memory, or -- on a device
+// that reads pageable host memory through the host's page tables (the
+// pageableMemoryAccessUsesHostPageTables attribute: coherent CPU-GPU
+// systems such as GB300 with its NVLink-C2C link) -- any host memory, read
+// in place at the link's rate instead of staged by the driver; anything
+// else is rejected before any launch.
 #include <algorithm>
 
 #include "sarbp_internal.cuh"
 
 namespace sarbp {
 
-// Device address of `src` for kernel loads, or nullptr when the memory is
-// not page-locked host memory with a mapping (or device memory).
-static const void *device_view(const void *src)
+// Whether the current device loads from and stores to pageable host memory
+// through the host's page tables (one query per device, cached).
+static bool reads_pageable()
+{
+    constexpr int kMaxDev = 64;
+    static int known[kMaxDev];                        // 0 unknown, 1 no, 2 yes
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) {
+        cudaGetLastError();
+        return false;
+    }
+    if (!known[dev]) {
+        int a = 0, b = 0;
+        const bool ok =
+            cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+                                   dev) == cudaSuccess;
+        if (!ok) cudaGetLastError();
+        known[dev] = ok && a && b ? 2 : 1;
+    }
+    return known[dev] == 2;
+}
+
+// Device address of host or device memory `p` for kernel loads and stores,
+// or nullptr when a kernel cannot reach it: page-locked host memory through
+// its mapping, device and managed memory as they are, pageable host memory
+// as it is on a device that reads it through the host's page tables.
+static const void *device_view(const void *p)
 {
     cudaPointerAttributes at;
-    if (cudaPointerGetAttributes(&at, src) != cudaSuccess) {
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
         cudaGetLastError();   // clear the sticky-free error of an unknown pointer
         return nullptr;
     }
-    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged)
-        return src;
+    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return p;
     if (at.type == cudaMemoryTypeHost) return at.devicePointer;
+    if (at.type == cudaMemoryTypeUnregistered && p && reads_pageable()) return p;
     return nullptr;
 }
 
@@ -279,13 +308,10 @@ int h2d_bytes(void *dst, const void *src, int64_t bytes, cudaStream_t stream)
 int d2h_bytes(void *dst, const void *src, int64_t bytes, cudaStream_t stream)
 {
     if (bytes <= 0) return SARBP_OK;
-    cudaPointerAttributes at;
-    if (cudaPointerGetAttributes(&at, dst) == cudaSuccess && at.type == cudaMemoryTypeHost &&
-        at.devicePointer) {
-        launch_copy_bytes(at.devicePointer, src, bytes, stream);
+    if (const void *dv = device_view(dst)) {
+        launch_copy_bytes(const_cast<void *>(dv), src, bytes, stream);
         return cuda_status(cudaGetLastError(), "device-to-host copy (SM stores)");
     }
-    cudaGetLastError();
     return cuda_status(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDeviceToHost, stream),
                        "device-to-host copy");
 }
@@ -350,6 +376,30 @@ extern "C" SARBP_API int sarbp_copy_to_device_sm(void *dst, const void *src, int
     }
     launch_copy_bytes(dst, sv, bytes, static_cast<cudaStream_t>(stream));
     return cuda_status(cudaGetLastError(), "sarbp_copy_to_device_sm launch");
+}
+
+extern "C" SARBP_API int sarbp_device_reads_pageable(void)
+{
+    return reads_pageable() ? 1 : 0;
+}
+
+extern "C" SARBP_API int sarbp_copy_to_host_sm(void *dst, const void *src, int64_t bytes,
+                                              void *stream)
+{
+    if (!dst || !src || bytes < 0) {
+        set_error("sarbp_copy_to_host_sm: NULL pointer or %lld bytes", (long long)bytes);
+        return SARBP_EINVAL;
+    }
+    if (bytes == 0) return SARBP_OK;
+    const void *dv = device_view(dst);
+    if (!dv) {
+        set_error("sarbp_copy_to_host_sm: the destination is neither page-locked host memory "
+                  "mapped into the device's address space nor host memory this device "
+                  "reaches through the host's page tables");
+        return SARBP_EINVAL;
+    }
+    launch_copy_bytes(const_cast<void *>(dv), src, bytes, static_cast<cudaStream_t>(stream));
+    return cuda_status(cudaGetLastError(), "sarbp_copy_to_host_sm launch");
 }
 
 extern "C" SARBP_API int sarbp_upload_host_arrays(int32_t n, void *const *dst,

@@ -141,7 +141,8 @@ def FocalizzatoreBpPx(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
         last_call.update(h2d_bytes=scene.h2d_bytes, d2h_bytes=img.nbytes,
                          raw_bins=(scene.bin_lo, scene.bin_hi), streamed=True,
                          upload=scene.upload,
-                         small_upload=getattr(scene, "small_upload", "per-array"))
+                         small_upload=getattr(scene, "small_upload", "per-array"),
+                         d2h=scene.d2h)
         return img
     scene = scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
                             near_range, dra, lambda_val, Sint, device=device, raw_bins="reached")
@@ -261,6 +262,9 @@ class _DropIn:
         self.out: dict[int, torch.Tensor] = {}
         self.small: dict[tuple, tuple] = {}
         self.images = FreshImages()
+        # kernels on this device read and write pageable host memory in place
+        with torch.cuda.device(dev):
+            self.pageable = bool(_lib.load().sarbp_device_reads_pageable())
 
     def small_buffers(self, npix: int, naz: int, dev) -> tuple:
         """One device buffer for the DEM, masks and trajectory of a scene
@@ -415,8 +419,9 @@ def _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache: _DropIn):
     host_rows = _pulse_major_host(args[8])
     # "signal": the bound is not waited for; the persistent block copy reads
     # it from page-locked memory once the stream has computed it
-    signal = (STREAM_UPLOAD == "signal" and host_rows is not None and host_rows.is_pinned()
-              and nra % 2 == 0 and host_rows.data_ptr() % 16 == 0)
+    reachable = host_rows is not None and (res_cache.pageable or host_rows.is_pinned())
+    signal = (STREAM_UPLOAD == "signal" and reachable and nra % 2 == 0
+              and host_rows.data_ptr() % 16 == 0)
     raw_buffer = res_cache.raw_buffer(nra, naz, dev)
     if not signal:
         scene = scene_to_device(*args, device=dev, raw_bins="bound", tuning=tq,
@@ -462,7 +467,7 @@ def _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache: _DropIn):
         lo, hi = read_bound(scene)           # the keys' synchronisation passed the bound
     else:
         lo, hi = scene.bin_lo, scene.bin_hi
-        sm = STREAM_UPLOAD in ("sm", "signal") and scene.host_rows.is_pinned()
+        sm = STREAM_UPLOAD in ("sm", "signal") and reachable
         copy = res_cache.copy_sm if sm else res_cache.copy
         upload = lib.sarbp_upload_raw_bins_sm if sm else lib.sarbp_upload_raw_bins
         copy.wait_stream(compute)           # raw buffer and tables allocated on compute
@@ -502,10 +507,17 @@ def _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache: _DropIn):
     res = FocusResult(image=out, workspace=ws)
     img = res_cache.images.get(scene.dim0, scene.dim1)
     # column-major pixels: the F-order array's memory is the device image's
-    dst = torch.from_numpy(img.reshape(-1, order="F").view(np.float64)).view(-1, 2)
-    dst.copy_(out)
-    del dst
-    res.check()
+    if res_cache.pageable:
+        # SM stores straight into the fresh array, in stream order
+        _lib.check(lib.sarbp_copy_to_host_sm(img.__array_interface__["data"][0],
+                                             out.data_ptr(), img.nbytes, compute.cuda_stream))
+        scene.d2h = "sm"
+    else:
+        dst = torch.from_numpy(img.reshape(-1, order="F").view(np.float64)).view(-1, 2)
+        dst.copy_(out)
+        del dst
+        scene.d2h = "copy"
+    res.check()                              # synchronises the stream
     return img, scene
 
 

@@ -124,20 +124,44 @@ def test_blocks_read_their_bound_from_memory(lib, where, bound):
     assert flags[:3].tolist() == [5, 5, 5]
 
 
-def test_pageable_source_is_rejected(lib):
-    src = np.zeros(4096, dtype=np.uint8)                 # not page-locked
+def test_pageable_memory_is_read_in_place_or_rejected(lib):
+    """Plain (pageable) host memory: on a device that reaches it through the
+    host's page tables every SM-load copy reads it in place and the SM-store
+    download writes it, with the copy engine's bytes; elsewhere each call
+    refuses it before any launch."""
+    rng = np.random.default_rng(3)
+    src = rng.integers(0, 256, 4096 + 64, dtype=np.uint8)
+    off = (-src.ctypes.data) % 16
+    src = src[off:off + 4096]                            # 16-byte aligned, not page-locked
     dst = torch.zeros(4096, dtype=torch.uint8, device="cuda")
-    rc = lib.sarbp_copy_to_device_sm(dst.data_ptr(), src.ctypes.data, 4096, _stream())
-    assert rc == _lib.SARBP_EINVAL and "page-locked" in _lib.last_error()
-    rc = lib.sarbp_upload_raw_bins_sm(dst.data_ptr(), 64, src.ctypes.data, 64, 0, 8, 8,
-                                      _stream())
-    assert rc == _lib.SARBP_EINVAL
-    ends = np.asarray([8], dtype=np.int64)
-    flags = torch.zeros(2, dtype=torch.int32, device="cuda")
-    rc = lib.sarbp_upload_raw_blocks_sm(dst.data_ptr(), 64, src.ctypes.data, 64, 0, 8,
-                                        ends.ctypes.data, 1, flags.data_ptr(),
-                                        flags.data_ptr() + 4, 1, 4, _stream())
-    assert rc == _lib.SARBP_EINVAL and "page-locked" in _lib.last_error()
+    ends = np.asarray([3, 8], dtype=np.int64)
+    flags = torch.zeros(4, dtype=torch.int32, device="cuda")
+    calls = [
+        lambda d: lib.sarbp_copy_to_device_sm(d.data_ptr(), src.ctypes.data, 4096, _stream()),
+        lambda d: lib.sarbp_upload_raw_bins_sm(d.data_ptr(), 64, src.ctypes.data, 64, 0, 64, 8,
+                                               _stream()),
+        lambda d: lib.sarbp_upload_raw_blocks_sm(d.data_ptr(), 64, src.ctypes.data, 64, 0, 64,
+                                                 ends.ctypes.data, 2, flags.data_ptr(),
+                                                 flags.data_ptr() + 8, 1, 4, _stream()),
+    ]
+    want = torch.from_numpy(src.copy())
+    if lib.sarbp_device_reads_pageable():
+        for call in calls:
+            dst.zero_()
+            _lib.check(call(dst))
+            torch.cuda.synchronize()
+            assert torch.equal(dst.cpu(), want)
+        back = np.zeros(4096 + 7, dtype=np.uint8)
+        _lib.check(lib.sarbp_copy_to_host_sm(back.ctypes.data + 7, dst.data_ptr(), 4096,
+                                             _stream()))
+        torch.cuda.synchronize()
+        assert np.array_equal(back[7:], src) and not back[:7].any()
+    else:
+        for call in calls:
+            assert call(dst) == _lib.SARBP_EINVAL and "page-locked" in _lib.last_error()
+        back = np.zeros(4096, dtype=np.uint8)
+        assert lib.sarbp_copy_to_host_sm(back.ctypes.data, dst.data_ptr(), 4096,
+                                         _stream()) == _lib.SARBP_EINVAL
 
 
 def _pinned_args(sc):

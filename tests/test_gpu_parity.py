@@ -15,7 +15,7 @@ import torch
 
 from conftest import GOLDEN, load_golden_scene
 from oracle import oracle
-from sar_backprojection_gb300 import focus, quality, scene_to_device, synth
+from sar_backprojection_gb300 import _lib, focus, quality, scene_to_device, synth
 
 pytestmark = pytest.mark.gpu
 
@@ -242,7 +242,8 @@ def test_full_workload_streamed_drop_in(full_scene, full_oracle, upload, pinned,
     the reachable range bins streamed up in pulse blocks while focusing runs
     (by each upload mode: SM loads per block, one persistent block copy that
     signals each block through a device flag, the copy engine; page-locked
-    raw rows, and pageable ones, which take the copy engine in every mode).
+    raw rows, and pageable ones, which the SM-load modes read in place on a
+    device that reaches pageable memory and the copy engine takes elsewhere).
     The returned image must equal the resident launch of the same tuning bit
     for bit (whose range bins equal the oracle's) and meet the bars against
     the oracle."""
@@ -262,8 +263,11 @@ def test_full_workload_streamed_drop_in(full_scene, full_oracle, upload, pinned,
     for _ in range(2):                                   # second call: next flag generation
         img = FocalizzatoreBpPx(*synth.focus_args(host), precision="mixed", tuning=tuning)
     assert focuser.last_call["streamed"]
-    assert focuser.last_call["upload"] == (upload if pinned else "copy")
-    if upload == "signal" and pinned:
+    # pageable rows take the copy engine unless the device reads pageable
+    # host memory in place
+    reachable = pinned or bool(_lib.load().sarbp_device_reads_pageable())
+    assert focuser.last_call["upload"] == (upload if reachable else "copy")
+    if upload == "signal" and reachable:
         assert focuser.last_call["small_upload"] == "one-call"
     assert img.shape == (4000, 250) and img.dtype == np.complex128
     ds = scene_to_device(*synth.focus_args(full_scene))
