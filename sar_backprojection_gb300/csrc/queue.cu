@@ -222,8 +222,15 @@ int Queue::admit(QJob &j)
 {
     const MixedLayout L = mixed_layout(j.P, T);
     j.ws_bytes = L.total;
-    int rc = queue_cuda(cudaMalloc(&j.ws, j.ws_bytes), "queue: scene workspace");
-    if (rc) return rc;
+    int rc = SARBP_OK;
+    if (j.arena_bytes) {
+        // carved from the reserved memory at admission: no cudaMalloc, and
+        // no device-wide synchronisation of a cudaFree when it retires
+        j.ws = arena.base + j.arena_off;
+    } else {
+        rc = queue_cuda(cudaMalloc(&j.ws, j.ws_bytes), "queue: scene workspace");
+        if (rc) return rc;
+    }
     rc = launch_mixed_prepare(j.P, T, j.ws, j.ws_bytes, stream[0]);
     if (rc) return rc;
     rc = tile_count(j.P, T, &j.ntiles);
@@ -357,15 +364,15 @@ bool Queue::advance_host()
 
 void Queue::finish(QJob &j)
 {
+    if (j.arena_bytes) arena.release(j.arena_off, j.arena_bytes);
     if (j.host) {
-        if (j.arena_bytes) arena.release(j.arena_off, j.arena_bytes);
-        j.arena_bytes = 0;
         j.ws = nullptr;
         if (j.ev) cudaEventDestroy(j.ev);
         j.ev = nullptr;
-    } else if (j.ws) {
+    } else if (j.ws && !j.arena_bytes) {
         cudaFree(j.ws);
     }
+    j.arena_bytes = 0;
     j.ws = nullptr;
     if (j.slot >= 0) free_slots.push_back(j.slot);
     j.slot = -1;
@@ -498,6 +505,15 @@ void Queue::run()
             while (!pending.empty() && !free_slots.empty()) {
                 QJob &j = *jobs[pending.front()];
                 if (j.host && !arena.alloc(j.arena_bytes, &j.arena_off)) break;
+                if (!j.host && arena.base) {
+                    // a device job's workspace comes from the reserved memory
+                    // when it fits there (else from cudaMalloc at admission)
+                    const size_t need = up256(mixed_layout(j.P, T).total);
+                    if (need <= arena.bytes) {
+                        if (!arena.alloc(need, &j.arena_off)) break;
+                        j.arena_bytes = need;
+                    }
+                }
                 pending.pop_front();
                 j.slot = free_slots.back();
                 free_slots.pop_back();
@@ -876,7 +892,8 @@ SARBP_API int sarbp_queue_destroy(sarbp_queue *queue)
     q.cv.notify_all();
     if (q.worker.joinable()) q.worker.join();
     for (auto &kv : q.jobs)
-        if (kv.second->ws && !kv.second->host) cudaFree(kv.second->ws);
+        if (kv.second->ws && !kv.second->host && !kv.second->arena_bytes)
+            cudaFree(kv.second->ws);
     for (int b = 0; b < 2; ++b) {
         if (q.stream[b]) cudaStreamDestroy(q.stream[b]);
         if (q.bws[b]) cudaFree(q.bws[b]);

@@ -578,6 +578,45 @@ class NativeServingEngine:
             if not j.nominal:
                 j.nominal = _nominal(j.args)
             prepared.append((j, sc, keep, out))
+
+        def submit(item):
+            j, sc, keep, out = item
+            return self.lib.sarbp_queue_submit_host(self._q, C.byref(sc), out.data_ptr())
+
+        def finished(item):
+            j, sc, keep, out = item
+            flat = out.numpy().view(np.complex128).reshape(-1)
+            j.image = np.reshape(flat, (sc.dim0, sc.dim1), order="F")
+
+        return self._drive(jobs, prepared, submit, finished, idle_sleep, timeout_s)
+
+    def run_resident(self, jobs: list, scene_of, idle_sleep: float = 5e-5,
+                     timeout_s: float = 600.0):
+        """The same loop for jobs whose inputs are already resident in device
+        memory (``scene_of(job)`` -> DeviceScene, sarbp_queue_submit): each
+        job's image goes to a device buffer of its own; admission by slot
+        and reserved memory (the chunk-table workspace is carved from it),
+        waves as for host jobs.  ``job.image`` is the (npix, 2) float64
+        device image."""
+        prepared = []
+        for j in sorted(jobs, key=lambda j: j.arrival):
+            sc = scene_of(j)
+            out = torch.empty((sc.npix, 2), dtype=torch.float64, device=sc.device)
+            if not j.nominal:
+                j.nominal = sc.nominal_pixel_pulses()
+            prepared.append((j, sc, out))
+        torch.cuda.synchronize(self.device)      # inputs and outputs exist before the worker
+
+        def submit(item):
+            j, sc, out = item
+            return self.lib.sarbp_queue_submit(self._q, C.byref(sc.struct()), out.data_ptr())
+
+        def finished(item):
+            item[0].image = item[2]
+
+        return self._drive(jobs, prepared, submit, finished, idle_sleep, timeout_s)
+
+    def _drive(self, jobs, prepared, submit, finished, idle_sleep, timeout_s):
         byid = {}
         before = self.stats()
         ids = (C.c_int64 * 256)()
@@ -593,20 +632,17 @@ class NativeServingEngine:
                 if now > timeout_s:
                     raise TimeoutError(f"serving run exceeded {timeout_s} s")
                 while nxt < len(prepared) and prepared[nxt][0].arrival <= now:
-                    j, sc, keep, out = prepared[nxt]
-                    jid = _lib.check(int(self.lib.sarbp_queue_submit_host(
-                        self._q, C.byref(sc), out.data_ptr())))
-                    j.admitted = now
+                    jid = _lib.check(int(submit(prepared[nxt])))
+                    prepared[nxt][0].admitted = now
                     byid[jid] = prepared[nxt]
                     nxt += 1
                 n = _lib.check(int(self.lib.sarbp_queue_completed(self._q, ids, times, stat,
                                                                   256)))
                 for k in range(n):
-                    j, sc, keep, out = byid.pop(ids[k])
+                    item = byid.pop(ids[k])
                     _lib.check(int(stat[k]))
-                    j.finished = times[k] - t0
-                    flat = out.numpy().view(np.complex128).reshape(-1)
-                    j.image = np.reshape(flat, (sc.dim0, sc.dim1), order="F")
+                    item[0].finished = times[k] - t0
+                    finished(item)
                 done += n
                 if n == 0 and idle_sleep:
                     wait = idle_sleep

@@ -133,3 +133,25 @@ def test_native_engine_reserved_memory_limits_residency(jobs):
         with pytest.raises(Exception) as e:
             eng.run(small[:1], timeout_s=30)
         assert "reserved" in str(e.value)
+
+
+@pytest.mark.parametrize("reserve", ["arena", "tiny"])
+def test_native_engine_resident_jobs_same_alone_and_in_the_mix(jobs, reserve):
+    """Device-resident inputs (sarbp_queue_submit) through the native loop:
+    each job's chunk-table workspace is carved from the reserved memory (or,
+    when the reserve cannot hold it, allocated at admission), and every
+    job's image equals its single-scene image bit for bit."""
+    tuning = batch.staged_tuning()
+    scenes = {j.job_id: scene_to_device(*j.args, device="cuda") for j in jobs}
+    mine = [serve.Job(job_id=j.job_id, arrival=j.arrival, args=j.args) for j in jobs]
+    budget = 4 * serve.GB if reserve == "arena" else 4096
+    with serve.NativeServingEngine(budget_bytes=budget, max_slots=8, wave_items=96,
+                                   tuning=tuning) as eng:
+        rep = eng.run_resident(mine, lambda j: scenes[j.job_id])
+    s = rep.summary()
+    assert s["completed"] == len(jobs) and s["h2d_gb"] == 0
+    for j, ref in zip(mine, jobs):
+        sc = scenes[j.job_id]
+        flat = j.image.cpu().numpy().view(np.complex128).reshape(-1)
+        img = np.reshape(flat, (sc.dim0, sc.dim1), order="F")
+        assert np.array_equal(_bits(img), _bits(_alone(ref, tuning))), f"job {j.job_id}"
