@@ -1,5 +1,5 @@
 /*
- * bp_oracle.c -- TEST INFRASTRUCTURE ONLY (the checker, never the product).
+ * bp_oracle.c -- TEST INFRASTRUCTURE ONLY (the oracle results are checked against; never the product).
  *
  * CPU FP64 restatement of the reference's per-pixel time-domain
  * back-projection.  Only tests/, __graft_entry__.smoke() and bench.py's CPU

@@ -1,4 +1,4 @@
-"""TEST INFRASTRUCTURE ONLY -- the oracle (checker) for the focuser.
+"""TEST INFRASTRUCTURE ONLY -- the oracle the focuser is checked against.
 
 ctypes wrapper of ``bp_oracle.c``, the CPU FP64 restatement of the reference's
 ``process_point`` / ``FocalizzatoreBpPx`` (sar_focuser_puntual_noui.py:9-284).
