@@ -54,4 +54,12 @@ __device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b)
     return d;
 }
 
+// max(a, b, c) in one three-input FP32 max (sm_100 and later).
+__device__ __forceinline__ float fmax3(float a, float b, float c)
+{
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 }  // namespace sarbp

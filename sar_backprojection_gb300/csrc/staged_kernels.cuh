@@ -521,7 +521,7 @@ __device__ __forceinline__ bool staged_tile(StagedCta &cta, const SceneParams &P
                                 float t0, t1, r0, r1;
                                 f2_unpack(t2, t0, t1);
                                 f2_unpack(r2, r0, r1);
-                                rmax = fmaxf(rmax, fmaxf(fabsf(r0), fabsf(r1)));
+                                rmax = fmax3(rmax, fabsf(r0), fabsf(r1));
                                 const int col0 = (int)min((unsigned)(__float_as_int(t0) + colbias),
                                                           (unsigned)(W - 1));
                                 const int col1 = (int)min((unsigned)(__float_as_int(t1) + colbias),
