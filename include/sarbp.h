@@ -281,7 +281,11 @@ SARBP_API int sarbp_upload_host_arrays(int32_t n, void *const *dst, const void *
  * ...UsesHostPageTables: coherent CPU-GPU systems such as GB300 over
  * NVLink-C2C), else 0.  On such a device every SM-load copy above also takes
  * plain (pageable) host memory, read in place at the link's rate rather than
- * staged by the driver.  No reference counterpart.
+ * staged by the driver.  A file mapping (mmap, np.memmap) is read too, but
+ * its pages not yet mapped are faulted in from the device one by one: copy
+ * such data into ordinary or page-locked memory first (the Python drop-in
+ * does this by leaving file mappings to the driver's staged copies).  No
+ * reference counterpart.
  */
 SARBP_API int sarbp_device_reads_pageable(void);
 

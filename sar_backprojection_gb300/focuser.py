@@ -349,13 +349,27 @@ _NP_OF = {torch.float64: np.dtype(np.float64), torch.uint8: np.dtype(np.uint8),
           torch.int32: np.dtype(np.int32)}
 
 
+def _file_backed(a) -> bool:
+    """Whether an array's memory is a file mapping (np.memmap, mmap): kernels
+    reading it in place would fault its pages in from the GPU one by one, so
+    such arrays take the driver's staged copies (CPU page-ins, readahead)."""
+    import mmap
+    seen = 0
+    while a is not None and seen < 32:
+        if isinstance(a, (np.memmap, mmap.mmap)):
+            return True
+        a = getattr(a, "base", None)
+        seen += 1
+    return False
+
+
 def _column_major_words(a, dt: torch.dtype, n: int, exact: bool):
     """Host address of an array of dtype ``dt`` whose column-major flatten
     (the reference's ``flatten(order='F')``) is its memory order, with n
     elements (at least n unless ``exact``); None otherwise."""
     if isinstance(a, np.ndarray):
         if (a.dtype != _NP_OF[dt] or not a.flags.f_contiguous
-                or (a.size != n if exact else a.size < n)):
+                or (a.size != n if exact else a.size < n) or _file_backed(a)):
             return None
         return a.__array_interface__["data"][0]
     if isinstance(a, torch.Tensor):
@@ -419,7 +433,10 @@ def _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache: _DropIn):
     host_rows = _pulse_major_host(args[8])
     # "signal": the bound is not waited for; the persistent block copy reads
     # it from page-locked memory once the stream has computed it
-    reachable = host_rows is not None and (res_cache.pageable or host_rows.is_pinned())
+    # rows kernels can load: page-locked, or pageable on a device that reads
+    # it in place (not a file mapping: see _file_backed)
+    reachable = host_rows is not None and (
+        host_rows.is_pinned() or (res_cache.pageable and not _file_backed(args[8])))
     signal = (STREAM_UPLOAD == "signal" and reachable and nra % 2 == 0
               and host_rows.data_ptr() % 16 == 0)
     raw_buffer = res_cache.raw_buffer(nra, naz, dev)

@@ -166,3 +166,18 @@ def test_one_call_upload_takes_only_arrays_that_need_no_conversion():
     assert _column_major_words(w, torch.float64, 10, False) is not None               # >= naz
     assert _column_major_words(w, torch.float64, 12, False) is None
     assert _column_major_words([1.0, 2.0], torch.float64, 2, False) is None
+
+
+def test_file_mappings_are_recognised(tmp_path):
+    """Memory-mapped inputs (and views of them) are kept off the in-place
+    pageable path; ordinary arrays are not."""
+    from sar_backprojection_gb300.focuser import _column_major_words, _file_backed
+
+    p = tmp_path / "a.dat"
+    np.zeros(24).tofile(p)
+    mm = np.memmap(p, dtype=np.float64, mode="r", shape=(6, 4), order="F")
+    assert _file_backed(mm) and _file_backed(mm.T) and _file_backed(mm[:, :2])
+    assert _file_backed(np.asarray(mm))
+    assert _column_major_words(mm, torch.float64, 24, True) is None
+    assert not _file_backed(np.zeros((6, 4))) and not _file_backed(None)
+    assert not _file_backed(np.array(mm, order="F"))         # a copy in ordinary memory
