@@ -107,3 +107,25 @@ def test_streamed_drop_in_equals_resident_focus(name):
     img2 = FocalizzatoreBpPx(*args, precision="mixed")
     assert np.array_equal(np.ascontiguousarray(img2).view(np.uint64),
                           np.ascontiguousarray(ref).view(np.uint64))
+
+
+def test_drop_in_from_memory_mapped_files(tmp_path):
+    """Inputs memory-mapped from .dat files (as the reference's large-scene
+    script maps them): the call takes the driver's staged copies for the
+    file-backed raw rows, never in-place device reads of the mapping, and
+    gives the in-memory call's image bit for bit."""
+    sc = SCENES["small"]()
+    args = _host_args(sc)
+    ref = FocalizzatoreBpPx(*args, precision="mixed")
+    raw = args[8]
+    mm = np.memmap(tmp_path / "raw_f.dat", dtype=np.complex64, mode="w+", shape=raw.shape,
+                   order="F")
+    mm[...] = raw
+    mm.flush()
+    mapped = list(args)
+    mapped[8] = np.memmap(tmp_path / "raw_f.dat", dtype=np.complex64, mode="r",
+                          shape=raw.shape, order="F")
+    img = FocalizzatoreBpPx(*mapped, precision="mixed")
+    assert focuser.last_call["streamed"] and focuser.last_call["upload"] == "copy"
+    assert np.array_equal(np.ascontiguousarray(img).view(np.uint64),
+                          np.ascontiguousarray(ref).view(np.uint64))
