@@ -200,12 +200,14 @@ gather_blocks16_kernel(float2 *__restrict__ dst, int64_t dpitch, const float2 *_
                 }
             }
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            __threadfence();                      // this CTA's rows before its count
-            if (atomicAdd(&counters[k], 1u) == gridDim.x - 1) {
-                __threadfence();
-                atomicExch(&flags[k], generation);
+        if (counters) {
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                __threadfence();                  // this CTA's rows before its count
+                if (atomicAdd(&counters[k], 1u) == gridDim.x - 1) {
+                    __threadfence();
+                    atomicExch(&flags[k], generation);
+                }
             }
         }
         a0 = a1;
@@ -303,6 +305,30 @@ int h2d_bytes(void *dst, const void *src, int64_t bytes, cudaStream_t stream)
     }
     return cuda_status(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyHostToDevice, stream),
                        "host copy");
+}
+
+// Rows [0, rows) of the bin interval that `bound` (int32[2], inclusive;
+// device or page-locked memory, written in stream order before the copy
+// runs) holds, by the four-row copy kernel on `ctas` CTAs, without
+// signalling.  SARBP_EINVAL (nothing enqueued) when the source, the
+// destination or the pitches do not suit its 16-byte words; the caller then
+// waits for the bound and uses h2d_rows.
+int h2d_rows_bound(float2 *dst, int64_t dpitch, const float2 *src, int64_t spitch,
+                   const int32_t *bound, int64_t rows, int ctas, cudaStream_t stream)
+{
+    if (rows <= 0) return SARBP_OK;
+    const void *sv = device_view(src);
+    const int *bv = static_cast<const int *>(device_view(bound));
+    if (!sv || !bv || (reinterpret_cast<uintptr_t>(sv) & 15) ||
+        (reinterpret_cast<uintptr_t>(dst) & 15) || (dpitch & 1) || (spitch & 1) || ctas <= 0)
+        return SARBP_EINVAL;
+    BlockEnds e{};
+    e.end[0] = rows;
+    const int64_t max_bins = dpitch < spitch ? dpitch : spitch;
+    gather_blocks16_kernel<<<ctas, kCopyThreads, 0, stream>>>(
+        dst, dpitch, static_cast<const float2 *>(sv), spitch, 0, 0, bv, max_bins, e, 1, nullptr,
+        nullptr, 0);
+    return cuda_status(cudaGetLastError(), "raw rows copy (SM loads, bound on the device)");
 }
 
 int d2h_bytes(void *dst, const void *src, int64_t bytes, cudaStream_t stream)

@@ -205,4 +205,8 @@ int h2d_bytes(void *dst, const void *src, int64_t bytes, cudaStream_t stream);
 int d2h_bytes(void *dst, const void *src, int64_t bytes, cudaStream_t stream);
 int h2d_rows(float2 *dst, int64_t dpitch, const float2 *src, int64_t spitch, int64_t lo,
              int64_t n, int64_t rows, cudaStream_t stream);
+// the same rows over the bin interval `bound` holds in memory (no host wait);
+// SARBP_EINVAL, nothing enqueued, when the layout does not suit it
+int h2d_rows_bound(float2 *dst, int64_t dpitch, const float2 *src, int64_t spitch,
+                   const int32_t *bound, int64_t rows, int ctas, cudaStream_t stream);
 }  // namespace sarbp
