@@ -132,15 +132,18 @@ def test_serving_engine_checks_its_options_before_the_device():
         serve.ServingEngine(device="cpu", policy="lifo")
 
 
-@pytest.mark.parametrize("naz,blocks,tail", [(40001, 8, 1), (40001, 8, 3), (2001, 4, 0),
-                                             (37, 8, 2), (40001, 30, 4)])
-def test_stream_marks_cover_the_pulses_with_a_short_tail(naz, blocks, tail):
+@pytest.mark.parametrize("naz,blocks,tail,head", [(40001, 8, 1, 0), (40001, 8, 3, 2),
+                                                  (2001, 4, 0, 0), (37, 8, 2, 3),
+                                                  (40001, 30, 4, 2)])
+def test_stream_marks_cover_the_pulses_with_a_short_tail(naz, blocks, tail, head):
     from sar_backprojection_gb300.focuser import _stream_marks
 
-    m = _stream_marks(naz, blocks, tail)
+    m = _stream_marks(naz, blocks, tail, head)
     assert m[-1] == naz and len(m) <= 32
     assert all(a <= b for a, b in zip(m, m[1:]))
-    if len(m) == blocks + tail:
+    if head and len(m) == blocks + tail + head:
+        assert m[0] == naz // (blocks << head)
+    if len(m) == blocks + tail + head:
         # the final blocks halve
         lens = np.diff([0] + m)
         assert all(lens[-1 - h] <= (naz // blocks) // (1 << h) + 1 for h in range(tail))
