@@ -424,7 +424,12 @@ extern "C" SARBP_API int sarbp_copy_to_host_sm(void *dst, const void *src, int64
                   "reaches through the host's page tables");
         return SARBP_EINVAL;
     }
-    launch_copy_bytes(const_cast<void *>(dv), src, bytes, static_cast<cudaStream_t>(stream));
+    const void *sv = device_view(src);
+    if (!sv) {
+        set_error("sarbp_copy_to_host_sm: the source is not memory the device can load from");
+        return SARBP_EINVAL;
+    }
+    launch_copy_bytes(const_cast<void *>(dv), sv, bytes, static_cast<cudaStream_t>(stream));
     return cuda_status(cudaGetLastError(), "sarbp_copy_to_host_sm launch");
 }
 
@@ -436,12 +441,22 @@ extern "C" SARBP_API int sarbp_upload_host_arrays(int32_t n, void *const *dst,
         set_error("sarbp_upload_host_arrays: %d arrays, or a NULL list", n);
         return SARBP_EINVAL;
     }
-    for (int32_t i = 0; i < n; ++i)
+    for (int32_t i = 0; i < n; ++i) {
         if (bytes[i] < 0 || (bytes[i] > 0 && (!dst[i] || !src[i]))) {
             set_error("sarbp_upload_host_arrays: array %d: NULL pointer or %lld bytes", i,
                       (long long)bytes[i]);
             return SARBP_EINVAL;
         }
+        cudaPointerAttributes at;
+        if (bytes[i] > 0 && (cudaPointerGetAttributes(&at, dst[i]) != cudaSuccess ||
+                             (at.type != cudaMemoryTypeDevice &&
+                              at.type != cudaMemoryTypeManaged))) {
+            cudaGetLastError();
+            set_error("sarbp_upload_host_arrays: array %d: the destination is not device "
+                      "memory", i);
+            return SARBP_EINVAL;
+        }
+    }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     for (int32_t i = 0; i < n; ++i) {
         const int rc = h2d_bytes(dst[i], src[i], bytes[i], s);

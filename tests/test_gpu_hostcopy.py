@@ -192,3 +192,33 @@ def test_serving_with_pinned_inputs_matches_alone(lib):
         ref = alone.to_numpy(ds.dim0, ds.dim1)
         assert np.array_equal(np.ascontiguousarray(j.image).view(np.uint64),
                               np.ascontiguousarray(ref).view(np.uint64)), f"job {j.job_id}"
+
+
+def test_upload_host_arrays_copies_each_and_checks_destinations(lib):
+    """One call, several arrays (page-locked, pageable, device sources, an
+    empty one): every destination gets its bytes; a host destination, or a
+    host source for the SM-store download, is refused before any copy."""
+    rng = np.random.default_rng(9)
+    pinned = torch.from_numpy(rng.integers(0, 256, 5000, dtype=np.uint8)).pin_memory()
+    plain = rng.integers(0, 256, 777, dtype=np.uint8)
+    dev_src = torch.from_numpy(rng.integers(0, 256, 4096, dtype=np.uint8)).cuda()
+    sizes = [5000, 777, 4096, 0]
+    dsts = [torch.zeros(max(n, 1), dtype=torch.uint8, device="cuda") for n in sizes]
+    srcs = [pinned.data_ptr(), plain.ctypes.data, dev_src.data_ptr(), pinned.data_ptr()]
+    dp = (C.c_void_p * 4)(*[d.data_ptr() for d in dsts])
+    sp = (C.c_void_p * 4)(*srcs)
+    nb = (C.c_int64 * 4)(*sizes)
+    _lib.check(lib.sarbp_upload_host_arrays(4, dp, sp, nb, _stream()))
+    torch.cuda.synchronize()
+    assert torch.equal(dsts[0].cpu(), pinned)
+    assert np.array_equal(dsts[1].cpu().numpy(), plain)
+    assert torch.equal(dsts[2], dev_src)
+    assert int(dsts[3].item()) == 0
+    host_dst = np.zeros(16, dtype=np.uint8)
+    bad = (C.c_void_p * 1)(host_dst.ctypes.data)
+    one = (C.c_void_p * 1)(pinned.data_ptr())
+    assert lib.sarbp_upload_host_arrays(1, bad, one, (C.c_int64 * 1)(16),
+                                        _stream()) == _lib.SARBP_EINVAL
+    assert "not device memory" in _lib.last_error()
+    out = torch.zeros(16, dtype=torch.uint8).pin_memory()
+    assert lib.sarbp_copy_to_host_sm(out.data_ptr(), 0x10, 16, _stream()) == _lib.SARBP_EINVAL
