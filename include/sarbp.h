@@ -281,7 +281,10 @@ SARBP_API int sarbp_upload_host_arrays(int32_t n, void *const *dst, const void *
  * ...UsesHostPageTables: coherent CPU-GPU systems such as GB300 over
  * NVLink-C2C), else 0.  On such a device every SM-load copy above also takes
  * plain (pageable) host memory, read in place at the link's rate rather than
- * staged by the driver.  A file mapping (mmap, np.memmap) is read too, but
+ * staged by the driver.  Such a range is checked on the host first: every
+ * page mapped (else SARBP_EINVAL), and each page a copy will write touched
+ * on the host, so a bad pointer fails there, not in a kernel.  A file
+ * mapping (mmap, np.memmap) is read too, but
  * its pages not yet mapped are faulted in from the device one by one: copy
  * such data into ordinary or page-locked memory first (the Python drop-in
  * does this by leaving file mappings to the driver's staged copies).  No

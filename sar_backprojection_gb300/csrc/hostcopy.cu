@@ -17,6 +17,9 @@
 // else is rejected before any launch.
 #include <algorithm>
 
+#include <sys/mman.h>
+#include <unistd.h>
+
 #include "sarbp_internal.cuh"
 
 namespace sarbp {
@@ -44,11 +47,34 @@ static bool reads_pageable()
     return known[dev] == 2;
 }
 
-// Device address of host or device memory `p` for kernel loads and stores,
-// or nullptr when a kernel cannot reach it: page-locked host memory through
-// its mapping, device and managed memory as they are, pageable host memory
-// as it is on a device that reads it through the host's page tables.
-static const void *device_view(const void *p)
+// Whether the pageable host range [p, p + bytes) may be handed to a kernel:
+// every page of it mapped in this process (msync fails with ENOMEM
+// otherwise), and, for a range the kernel will write, every page touched
+// here first (read and written back), so an unmapped or read-only
+// destination fails on the host, never as a device fault.
+static bool pageable_range_ok(const void *p, int64_t bytes, bool write)
+{
+    if (!p || bytes <= 0) return false;
+    const uintptr_t pg = (uintptr_t)sysconf(_SC_PAGESIZE);
+    const uintptr_t b = reinterpret_cast<uintptr_t>(p), e = b + (uintptr_t)bytes;
+    if (pg == 0 || (pg & (pg - 1)) || e < b) return false;
+    const uintptr_t a = b & ~(pg - 1);
+    if (msync(reinterpret_cast<void *>(a), e - a, MS_ASYNC) != 0) return false;
+    if (write)
+        for (uintptr_t q = b; q < e; q = (q & ~(pg - 1)) + pg) {
+            volatile unsigned char *c = reinterpret_cast<volatile unsigned char *>(q);
+            const unsigned char v = *c;
+            *c = v;
+        }
+    return true;
+}
+
+// Device address of host or device memory `p` for kernel loads (stores when
+// `write`) over `bytes` bytes, or nullptr when a kernel cannot reach it:
+// page-locked host memory through its mapping, device and managed memory as
+// they are, pageable host memory as it is on a device that reads it through
+// the host's page tables, once the range has been checked on the host.
+static const void *device_view(const void *p, int64_t bytes, bool write = false)
 {
     cudaPointerAttributes at;
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
@@ -57,7 +83,9 @@ static const void *device_view(const void *p)
     }
     if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return p;
     if (at.type == cudaMemoryTypeHost) return at.devicePointer;
-    if (at.type == cudaMemoryTypeUnregistered && p && reads_pageable()) return p;
+    if (at.type == cudaMemoryTypeUnregistered && reads_pageable() &&
+        pageable_range_ok(p, bytes, write))
+        return p;
     return nullptr;
 }
 
@@ -299,7 +327,7 @@ static void launch_copy_bytes(void *dst, const void *sv, int64_t bytes, cudaStre
 int h2d_bytes(void *dst, const void *src, int64_t bytes, cudaStream_t stream)
 {
     if (bytes <= 0) return SARBP_OK;
-    if (const void *sv = device_view(src)) {
+    if (const void *sv = device_view(src, bytes)) {
         launch_copy_bytes(dst, sv, bytes, stream);
         return cuda_status(cudaGetLastError(), "host copy (SM loads)");
     }
@@ -317,8 +345,8 @@ int h2d_rows_bound(float2 *dst, int64_t dpitch, const float2 *src, int64_t spitc
                    const int32_t *bound, int64_t rows, int ctas, cudaStream_t stream)
 {
     if (rows <= 0) return SARBP_OK;
-    const void *sv = device_view(src);
-    const int *bv = static_cast<const int *>(device_view(bound));
+    const void *sv = device_view(src, rows * spitch * (int64_t)sizeof(float2));
+    const int *bv = static_cast<const int *>(device_view(bound, 2 * sizeof(int32_t)));
     if (!sv || !bv || (reinterpret_cast<uintptr_t>(sv) & 15) ||
         (reinterpret_cast<uintptr_t>(dst) & 15) || (dpitch & 1) || (spitch & 1) || ctas <= 0)
         return SARBP_EINVAL;
@@ -334,7 +362,7 @@ int h2d_rows_bound(float2 *dst, int64_t dpitch, const float2 *src, int64_t spitc
 int d2h_bytes(void *dst, const void *src, int64_t bytes, cudaStream_t stream)
 {
     if (bytes <= 0) return SARBP_OK;
-    if (const void *dv = device_view(dst)) {
+    if (const void *dv = device_view(dst, bytes, true)) {
         launch_copy_bytes(const_cast<void *>(dv), src, bytes, stream);
         return cuda_status(cudaGetLastError(), "device-to-host copy (SM stores)");
     }
@@ -346,7 +374,7 @@ int h2d_rows(float2 *dst, int64_t dpitch, const float2 *src, int64_t spitch, int
              int64_t n, int64_t rows, cudaStream_t stream)
 {
     if (n <= 0 || rows <= 0) return SARBP_OK;
-    if (const void *sv = device_view(src)) {
+    if (const void *sv = device_view(src, rows * spitch * (int64_t)sizeof(float2))) {
         launch_rows(dst, dpitch, static_cast<const float2 *>(sv), spitch, lo, n, rows, 4,
                     stream);
         return cuda_status(cudaGetLastError(), "raw rows copy (SM loads)");
@@ -375,7 +403,7 @@ extern "C" SARBP_API int sarbp_upload_raw_bins_sm(void *dst, int64_t dst_pitch, 
         return SARBP_EINVAL;
     }
     if (nbins == 0 || npulses == 0) return SARBP_OK;
-    const void *sv = device_view(src);
+    const void *sv = device_view(src, npulses * src_pitch * (int64_t)sizeof(float2));
     if (!sv) {
         set_error("sarbp_upload_raw_bins_sm: the source is not page-locked host memory mapped "
                   "into the device's address space (or device memory)");
@@ -394,7 +422,7 @@ extern "C" SARBP_API int sarbp_copy_to_device_sm(void *dst, const void *src, int
         return SARBP_EINVAL;
     }
     if (bytes == 0) return SARBP_OK;
-    const void *sv = device_view(src);
+    const void *sv = device_view(src, bytes);
     if (!sv) {
         set_error("sarbp_copy_to_device_sm: the source is not page-locked host memory mapped "
                   "into the device's address space (or device memory)");
@@ -417,14 +445,14 @@ extern "C" SARBP_API int sarbp_copy_to_host_sm(void *dst, const void *src, int64
         return SARBP_EINVAL;
     }
     if (bytes == 0) return SARBP_OK;
-    const void *dv = device_view(dst);
+    const void *dv = device_view(dst, bytes, true);
     if (!dv) {
         set_error("sarbp_copy_to_host_sm: the destination is neither page-locked host memory "
                   "mapped into the device's address space nor host memory this device "
                   "reaches through the host's page tables");
         return SARBP_EINVAL;
     }
-    const void *sv = device_view(src);
+    const void *sv = device_view(src, bytes);
     if (!sv) {
         set_error("sarbp_copy_to_host_sm: the source is not memory the device can load from");
         return SARBP_EINVAL;
@@ -489,7 +517,7 @@ static int upload_blocks(const char *who, void *dst, int64_t dst_pitch, const vo
         }
         e.end[k] = prev = block_ends[k];
     }
-    const void *sv = device_view(src);
+    const void *sv = device_view(src, prev * src_pitch * (int64_t)sizeof(float2));
     if (!sv || (reinterpret_cast<uintptr_t>(sv) & 15)) {
         set_error("%s: the source is not 16-byte aligned page-locked host memory mapped into "
                   "the device's address space (or device memory)", who);
@@ -497,7 +525,7 @@ static int upload_blocks(const char *who, void *dst, int64_t dst_pitch, const vo
     }
     const int *bv = nullptr;
     if (bound) {
-        bv = static_cast<const int *>(device_view(bound));
+        bv = static_cast<const int *>(device_view(bound, 2 * sizeof(int32_t)));
         if (!bv) {
             set_error("%s: the bound is neither device memory nor page-locked host memory", who);
             return SARBP_EINVAL;

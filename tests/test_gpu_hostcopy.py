@@ -222,3 +222,35 @@ def test_upload_host_arrays_copies_each_and_checks_destinations(lib):
     assert "not device memory" in _lib.last_error()
     out = torch.zeros(16, dtype=torch.uint8).pin_memory()
     assert lib.sarbp_copy_to_host_sm(out.data_ptr(), 0x10, 16, _stream()) == _lib.SARBP_EINVAL
+
+
+def test_unmapped_host_ranges_are_refused_on_the_host(lib):
+    """A host range with an unmapped page in it (or a stray address) is
+    refused by the copy entry points before any launch, also on a device
+    that reads pageable memory in place (the range is checked on the host
+    first)."""
+    import mmap as _mmap
+    libc = C.CDLL(None, use_errno=True)
+    libc.mmap.restype = C.c_void_p
+    libc.mmap.argtypes = [C.c_void_p, C.c_size_t, C.c_int, C.c_int, C.c_int, C.c_long]
+    libc.munmap.argtypes = [C.c_void_p, C.c_size_t]
+    pg = _mmap.PAGESIZE
+    base = libc.mmap(None, 3 * pg, _mmap.PROT_READ | _mmap.PROT_WRITE,
+                     _mmap.MAP_PRIVATE | _mmap.MAP_ANONYMOUS, -1, 0)
+    assert base not in (None, C.c_void_p(-1).value)
+    try:
+        assert libc.munmap(base + pg, pg) == 0          # a hole in the middle
+        dst = torch.zeros(3 * pg, dtype=torch.uint8, device="cuda")
+        rc = lib.sarbp_copy_to_device_sm(dst.data_ptr(), base, 3 * pg, _stream())
+        assert rc == _lib.SARBP_EINVAL
+        rc = lib.sarbp_copy_to_host_sm(base, dst.data_ptr(), 3 * pg, _stream())
+        assert rc == _lib.SARBP_EINVAL
+        # the mapped first page alone is fine where pageable memory is reachable
+        rc = lib.sarbp_copy_to_device_sm(dst.data_ptr(), base, pg, _stream())
+        assert rc == (_lib.SARBP_OK if lib.sarbp_device_reads_pageable() else _lib.SARBP_EINVAL)
+        torch.cuda.synchronize()
+        assert lib.sarbp_copy_to_device_sm(dst.data_ptr(), 0x10, 16,
+                                           _stream()) == _lib.SARBP_EINVAL
+    finally:
+        libc.munmap(base, pg)
+        libc.munmap(base + 2 * pg, pg)
