@@ -20,10 +20,22 @@ import torch
 from . import _lib
 
 
+def _host_view(a: np.ndarray) -> torch.Tensor:
+    """torch view of a host array's memory.  Read-only arrays (memory maps,
+    buffers) are only ever read here, so torch's warning about them is
+    silenced."""
+    if a.flags.writeable:
+        return torch.from_numpy(a)
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", UserWarning)
+        return torch.from_numpy(a)
+
+
 def _as_tensor(a) -> torch.Tensor:
     if isinstance(a, torch.Tensor):
         return a
-    return torch.from_numpy(np.asarray(a))
+    return _host_view(np.asarray(a))
 
 
 def _cast_host(a, np_dtype):
@@ -70,7 +82,7 @@ def raw_to_device(raw, device, pitch_multiple: int = 2) -> tuple[torch.Tensor, i
         arr = np.asarray(raw)
         if arr.dtype != np.complex64:
             arr = arr.astype(np.complex64)
-        t = torch.from_numpy(arr)
+        t = _host_view(arr)
     if t.dim() != 2:
         raise ValueError("Raw_Data must be a 2D array")
     nra, naz = int(t.shape[0]), int(t.shape[1])
@@ -175,7 +187,7 @@ def _pulse_major_host(raw):
         a = np.asarray(raw)
         if a.dtype != np.complex64 or not a.flags.f_contiguous:
             return None
-        t = torch.from_numpy(a.T)
+        t = _host_view(a.T)
     return t if t.is_contiguous() else None
 
 
