@@ -16,12 +16,18 @@
 // fit in the queue's reserved device memory (first fit, in arrival order),
 // their small inputs go up, their chunk tables and the bound of the range
 // bins their apertures can reach are computed on a setup stream (the bound
-// lands in pinned memory); once the worker sees that, only the reachable
-// bins of each pulse row are copied on a copy stream; once those have
-// landed the job's tiles join waves; after its last wave its image goes
-// back to the caller's host buffer on a read-back stream.  Page-locked
-// sources and destinations are copied by SM loads / asynchronously, so no
-// step makes the worker wait for the GPU; it polls events between steps.
+// lands in pinned memory); only the reachable bins of each pulse row are
+// then copied on a copy stream, queued at admission behind the set-up (a
+// device-side wait) by a copy kernel that reads the bound itself, so no
+// host round trip separates one job's bound from its upload (layouts that
+// kernel cannot take wait for the bound on the host instead); once the rows
+// have landed the job's tiles join waves; after its last wave its image
+// goes back to the caller's host buffer on a read-back stream.  Sources and
+// destinations the device can reach (page-locked memory, and on GB300 any
+// host memory) are copied by SM loads and stores, so no step makes the
+// worker wait for the GPU; it polls events between steps.  Device-resident
+// jobs take their chunk-table workspace from the reserved memory too when
+// it is reserved.
 #include <algorithm>
 #include <condition_variable>
 #include <chrono>
