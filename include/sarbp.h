@@ -333,6 +333,9 @@ SARBP_API int sarbp_upload_raw_blocks_bound_sm(void *dst, int64_t dst_pitch, con
                                                uint32_t *flags, uint32_t *counters,
                                                uint32_t generation, int32_t ctas, void *stream);
 SARBP_API int sarbp_stream_wait_flag(void *stream, const uint32_t *flag, uint32_t value);
+/* 1 when the driver provides the stream wait sarbp_stream_wait_flag uses
+ * (cuStreamWaitValue32), else 0: callers fall back to event ordering. */
+SARBP_API int sarbp_stream_wait_supported(void);
 
 /*
  * Batches: many scenes of uneven size in one persistent launch.

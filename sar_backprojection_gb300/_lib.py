@@ -110,6 +110,7 @@ SIGNATURES = {
                                                    C.c_int32, _P, _P, C.c_uint32, C.c_int32,
                                                    _P]),
     "sarbp_stream_wait_flag": (C.c_int, [_P, _P, C.c_uint32]),
+    "sarbp_stream_wait_supported": (C.c_int, []),
     "sarbp_upload_host_arrays": (C.c_int, [C.c_int32, _P, _P, _P, _P]),
     "sarbp_device_reads_pageable": (C.c_int, []),
     "sarbp_copy_to_host_sm": (C.c_int, [_P, _P, C.c_int64, _P]),

@@ -591,6 +591,11 @@ WaitValueFn wait_value_fn()
 }
 }  // namespace
 
+extern "C" SARBP_API int sarbp_stream_wait_supported(void)
+{
+    return wait_value_fn() ? 1 : 0;
+}
+
 extern "C" SARBP_API int sarbp_stream_wait_flag(void *stream, const uint32_t *flag, uint32_t value)
 {
     if (!flag) {

@@ -266,6 +266,8 @@ class _DropIn:
         # kernels on this device read and write pageable host memory in place
         with torch.cuda.device(dev):
             self.pageable = bool(_lib.load().sarbp_device_reads_pageable())
+        # "signal" uploads need the driver's stream wait on a memory value
+        self.wait_ok = bool(_lib.load().sarbp_stream_wait_supported())
 
     def small_buffers(self, npix: int, naz: int, dev) -> tuple:
         """One device buffer for the DEM, masks and trajectory of a scene
@@ -440,7 +442,7 @@ def _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache: _DropIn):
     # it in place (not a file mapping: see _file_backed)
     reachable = host_rows is not None and (
         host_rows.is_pinned() or (res_cache.pageable and not _file_backed(args[8])))
-    signal = (STREAM_UPLOAD == "signal" and reachable and nra % 2 == 0
+    signal = (STREAM_UPLOAD == "signal" and res_cache.wait_ok and reachable and nra % 2 == 0
               and host_rows.data_ptr() % 16 == 0)
     raw_buffer = res_cache.raw_buffer(nra, naz, dev)
     if not signal:
