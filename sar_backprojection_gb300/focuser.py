@@ -142,7 +142,7 @@ def FocalizzatoreBpPx(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
                          raw_bins=(scene.bin_lo, scene.bin_hi), streamed=True,
                          upload=scene.upload,
                          small_upload=getattr(scene, "small_upload", "per-array"),
-                         d2h=scene.d2h)
+                         d2h=scene.d2h, launches=scene.launches)
         return img
     scene = scene_to_device(xxg1, yyg1, zzg1, mask, index, wgsx, wgsy, wgsz, Raw_Data,
                             near_range, dra, lambda_val, Sint, device=device, raw_bins="reached")
@@ -418,6 +418,10 @@ def _scene_from_host(args, dev, lib, res_cache: _DropIn, raw_buffer, host_rows):
     scene.h2d_bytes = total
     scene.host_rows = host_rows
     scene.small_upload = "one-call"
+    # copy kernels among the nine copies (the rest went through the driver)
+    scene.small_kernels = 9 if res_cache.pageable else sum(
+        1 for a in (xxg1, yyg1, zzg1, mask, index, sint, wgsx, wgsy, wgsz)
+        if isinstance(a, torch.Tensor) and a.is_pinned())
     return scene
 
 
@@ -496,6 +500,9 @@ def _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache: _DropIn):
     row = scene.pitch * 8
     first = 0
     a0 = 0
+    # this library's kernels the call launches: chunk tables, the bound (3),
+    # the queue keys, the small-input copies, then per block below
+    launches = 1 + 3 + 1 + getattr(scene, "small_kernels", 0) + (1 if signal else 0)
     for k in range(len(marks)):
         a1 = marks[k]
         lane = lanes[k % len(lanes)]
@@ -510,6 +517,7 @@ def _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache: _DropIn):
                     scene.raw.data_ptr() + a0 * row, scene.pitch,
                     scene.host_rows.data_ptr() + a0 * scene.nra * 8, scene.nra, lo,
                     hi - lo + 1, a1 - a0, copy.cuda_stream))
+                launches += 1 if sm else 0
             ev = torch.cuda.Event()
             ev.record(copy)
             lane.wait_event(ev)
@@ -518,6 +526,7 @@ def _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache: _DropIn):
             _lib.check(lib.sarbp_focus_mixed_range(sc, C.byref(tq), out.data_ptr(), None, None,
                                                    None, ws.data_ptr(), ws.numel(), first,
                                                    count, lane.cuda_stream))
+            launches += 1
         first = int(ends[k])
         a0 = a1
     if hi >= lo:
@@ -534,12 +543,14 @@ def _focus_streamed_locked(args, tq, dev, blocks, lib, res_cache: _DropIn):
         _lib.check(lib.sarbp_copy_to_host_sm(img.__array_interface__["data"][0],
                                              out.data_ptr(), img.nbytes, compute.cuda_stream))
         scene.d2h = "sm"
+        launches += 1
     else:
         dst = torch.from_numpy(img.reshape(-1, order="F").view(np.float64)).view(-1, 2)
         dst.copy_(out)
         del dst
         scene.d2h = "copy"
     res.check()                              # synchronises the stream
+    scene.launches = launches
     return img, scene
 
 
