@@ -74,14 +74,19 @@ def parse():
     ap.add_argument("--large-scene", type=int, default=1,
                     help="1: also run the large-scene driver at the reference's 4000 x 32000 "
                          "DEM / 403484-pulse size (needs ~45 GB of disk and host memory)")
-    ap.add_argument("--workload", choices=["full", "profile"], default="full",
+    ap.add_argument("--workload", choices=["full", "profile", "small"], default="full",
                     help="profile: the same geometry at 1000x250 pixels / 10001 pulses "
-                         "(381 MB of raw data), a small case for ncu captures")
+                         "(381 MB of raw data), a small case for ncu captures; small: the "
+                         "reference's 256x64 / 2001-pulse CPU case")
     return ap.parse_args()
 
 
 def workload_spec(args, rank: int):
     from sar_backprojection_gb300 import synth
+    if args.workload == "small":
+        return (synth.config_small(args.seed + rank),
+                "small_256x64_2001: DEM 256x64 at 1 m, flat, 2001 pulses, Nra 512, Sint 400, "
+                "8 point targets + noise at 20 dB (the reference's CPU-runnable case)")
     if args.workload == "profile":
         return (synth.scaled_full(args.seed + rank, 1000, 250, 10001, 1200, 1800,
                                   name="profile_1000x250_10001"),
